@@ -1,0 +1,337 @@
+/*
+ * ogl_beamformer_lib.h -- C ABI of the GB300 beamforming library.
+ *
+ * Drop-in for the client library of the reference beamformer
+ * (helpers/ogl_beamformer_lib_base.h + beamformer_parameters.h, concatenated into
+ * one header by build.c:659-671 in the reference). Every type, enum value and
+ * function signature below keeps the reference's binary contract so that existing
+ * callers (MATLAB loadlibrary, C test drivers) link against this library unchanged.
+ *
+ * Differences in *transport*: the reference library talks to a separate `ogl`
+ * server process through a 2 GB POSIX shared-memory region and futex locks
+ * (helpers/ogl_beamformer_lib.c:30-125). This library runs the whole pipeline
+ * in-process on one GB300: pushes copy the caller's data to device memory, compute
+ * is launched on a CUDA stream, and the `timeout_ms` arguments bound the waits on
+ * that stream instead of waits on shared-memory locks.
+ *
+ * All functions are C ABI (`extern "C"`), take plain pointers and sizes, and are
+ * not thread safe (one process-global context, as in the reference).
+ */
+#ifndef OGL_BEAMFORMER_LIB_H
+#define OGL_BEAMFORMER_LIB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifndef LIB_FN
+  #if defined(_WIN32)
+    #define LIB_FN __declspec(dllexport)
+  #else
+    #define LIB_FN __attribute__((visibility("default")))
+  #endif
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------------
+ * Shader (stage) kinds. Values are the reference's (beamformer_parameters.h:14-41).
+ * Kinds 8..13 are internal variants chosen by pipeline planning; callers push
+ * kinds 0..7.
+ * ---------------------------------------------------------------------------- */
+typedef enum {
+	BeamformerShaderKind_CudaDecode         = 0,
+	BeamformerShaderKind_CudaHilbert        = 1,
+	BeamformerShaderKind_DAS                = 2,
+	BeamformerShaderKind_Decode             = 3,
+	BeamformerShaderKind_Filter             = 4,
+	BeamformerShaderKind_Demodulate         = 5,
+	BeamformerShaderKind_MinMax             = 6,
+	BeamformerShaderKind_Sum                = 7,
+	BeamformerShaderKind_DecodeInt16Complex = 8,
+	BeamformerShaderKind_DecodeFloat        = 9,
+	BeamformerShaderKind_DecodeFloatComplex = 10,
+	BeamformerShaderKind_DecodeInt16ToFloat = 11,
+	BeamformerShaderKind_DemodulateFloat    = 12,
+	BeamformerShaderKind_DASFast            = 13,
+	BeamformerShaderKind_Render3D           = 14,
+	BeamformerShaderKind_Count              = 15,
+
+	BeamformerShaderKind_ComputeCount = BeamformerShaderKind_Render3D,
+} BeamformerShaderKind;
+
+/* Per-frame stage timings in seconds, last 32 computes (beamformer_parameters.h:43-48). */
+typedef struct {
+	float times[32][BeamformerShaderKind_Count];
+	float rf_time_deltas[32];
+} BeamformerComputeStatsTable;
+
+/* Decode modes (beamformer_parameters.h:51-53). */
+enum { DECODE_MODE_NONE = 0, DECODE_MODE_HADAMARD = 1 };
+
+/* Input data kinds (beamformer_parameters.h:55-63). */
+typedef enum {
+	BeamformerDataKind_Int16          = 0,
+	BeamformerDataKind_Int16Complex   = 1,
+	BeamformerDataKind_Float32        = 2,
+	BeamformerDataKind_Float32Complex = 3,
+} BeamformerDataKind;
+
+/* Filter kinds (beamformer_parameters.h:65-71). */
+typedef enum {
+	BeamformerFilterKind_Kaiser  = 0,
+	BeamformerFilterKind_Matched = 1,
+} BeamformerFilterKind;
+
+/* Image plane tags (beamformer_parameters.h:74-85). */
+typedef enum {
+	BeamformerViewPlaneTag_XZ        = 0,
+	BeamformerViewPlaneTag_YZ        = 1,
+	BeamformerViewPlaneTag_XY        = 2,
+	BeamformerViewPlaneTag_Arbitrary = 3,
+	BeamformerViewPlaneTag_Count,
+} BeamformerViewPlaneTag;
+
+/* Delay-and-sum kinds, stored in BeamformerParameters.das_shader_id
+ * (beamformer_parameters.h:88-99). */
+typedef enum {
+	DASShaderKind_FORCES         = 0,
+	DASShaderKind_UFORCES        = 1,
+	DASShaderKind_HERCULES       = 2,
+	DASShaderKind_RCA_VLS        = 3,
+	DASShaderKind_RCA_TPW        = 4,
+	DASShaderKind_UHERCULES      = 5,
+	DASShaderKind_RACES          = 6,
+	DASShaderKind_EPIC_FORCES    = 7,
+	DASShaderKind_EPIC_UFORCES   = 8,
+	DASShaderKind_EPIC_UHERCULES = 9,
+	DASShaderKind_FLASH          = 10,
+	DASShaderKind_Count,
+} DASShaderKind;
+
+#define MAX_BEAMFORMED_SAVED_FRAMES 16   /* beamformer_parameters.h:127 */
+#define MAX_COMPUTE_SHADER_STAGES   16   /* beamformer_parameters.h:128 */
+#define BEAMFORMER_FILTER_SLOTS      4   /* beamformer_parameters.h:130 */
+
+/* ------------------------------------------------------------------------------
+ * Parameter block. std140-compatible, 208 bytes, field order and offsets exactly
+ * as the reference's X-macro expansion (beamformer_parameters.h:134-175):
+ *   xdc_transform 0, dec_data_dim 64, xdc_element_pitch 80, rf_raw_dim 88,
+ *   transmit_mode 96, decode 100, das_shader_id 104, time_offset 108,
+ *   output_min_coordinate 112, output_max_coordinate 128, output_points 144,
+ *   sampling_frequency 160, center_frequency 164, speed_of_sound 168,
+ *   off_axis_pos 172, beamform_plane 176, f_number 180, interpolate 184,
+ *   coherency_weighting 188, decimation_rate 192, readi_group_id 196,
+ *   readi_group_size 200.
+ * ---------------------------------------------------------------------------- */
+#define BF_PARAMETERS_UI_FIELDS \
+	float    output_min_coordinate[4]; /* [m] back-top-left corner of the output region */ \
+	float    output_max_coordinate[4]; /* [m] front-bottom-right corner of the output region */ \
+	int32_t  output_points[4];         /* width, height, depth, frames to average */ \
+	float    sampling_frequency;       /* [Hz] */ \
+	float    center_frequency;         /* [Hz] */ \
+	float    speed_of_sound;           /* [m/s] */ \
+	float    off_axis_pos;             /* [m] plane position normal to the beamformed plane */ \
+	int32_t  beamform_plane;           /* plane to beamform in TPW/VLS/HERCULES */ \
+	float    f_number;                 /* receive F# (0 disables apodization) */ \
+	uint32_t interpolate;              /* cubic interpolation of RF samples */ \
+	uint32_t coherency_weighting;      /* coherency-weighted output */
+
+#define BF_PARAMETERS_HEAD_FIELDS \
+	float    xdc_transform[16];        /* column-major array transform */ \
+	uint32_t dec_data_dim[4];          /* samples, channels, transmits; last ignored */ \
+	float    xdc_element_pitch[2];     /* [m] element pitch {row, col} */ \
+	uint32_t rf_raw_dim[2];            /* raw data dimensions */ \
+	int32_t  transmit_mode;            /* transmit/receive orientation bits */ \
+	uint32_t decode;                   /* DECODE_MODE_* */ \
+	uint32_t das_shader_id;            /* DASShaderKind */ \
+	float    time_offset;              /* [s] pulse length correction */
+
+#define BF_PARAMETERS_TAIL_FIELDS \
+	uint32_t decimation_rate;          /* decimation of the demodulation stage */ \
+	uint32_t readi_group_id;           /* READI group of this data */ \
+	uint32_t readi_group_size;         /* READI transmit group size */
+
+typedef struct { BF_PARAMETERS_UI_FIELDS   } BeamformerUIParameters;
+typedef struct { BF_PARAMETERS_HEAD_FIELDS } BeamformerParametersHead;
+typedef struct { BF_PARAMETERS_TAIL_FIELDS } BeamformerParametersTail;
+
+typedef struct {
+	BF_PARAMETERS_HEAD_FIELDS
+	BF_PARAMETERS_UI_FIELDS
+	BF_PARAMETERS_TAIL_FIELDS
+	float _pad[1];
+} BeamformerParameters;
+
+#if defined(__cplusplus)
+static_assert(sizeof(BeamformerParameters) == 208, "BeamformerParameters must be 208 bytes");
+static_assert(offsetof(BeamformerParameters, output_min_coordinate) == 112, "UI block offset");
+static_assert(offsetof(BeamformerParameters, decimation_rate) == 192, "tail block offset");
+#elif defined(__STDC_VERSION__) && __STDC_VERSION__ >= 201112L
+_Static_assert(sizeof(BeamformerParameters) == 208, "BeamformerParameters must be 208 bytes");
+_Static_assert(offsetof(BeamformerParameters, output_min_coordinate) == 112, "UI block offset");
+_Static_assert(offsetof(BeamformerParameters, decimation_rate) == 192, "tail block offset");
+#endif
+
+/* Live-imaging dirty flags and parameters (beamformer_parameters.h:184-202). */
+typedef enum {
+	BeamformerLiveImagingDirtyFlags_ImagePlaneOffsets = 1 << 0,
+	BeamformerLiveImagingDirtyFlags_TransmitPower     = 1 << 1,
+	BeamformerLiveImagingDirtyFlags_TGCControlPoints  = 1 << 2,
+	BeamformerLiveImagingDirtyFlags_SaveData          = 1 << 3,
+	BeamformerLiveImagingDirtyFlags_StopImaging       = 1 << 4,
+} BeamformerLiveImagingDirtyFlags;
+
+typedef struct {
+	uint32_t active;
+	uint32_t save_enabled;
+	uint32_t save_active;
+	float    transmit_power;
+	float    image_plane_offsets[BeamformerViewPlaneTag_Count];
+	float    tgc_control_points[8];
+} BeamformerLiveImagingParameters;
+
+/* ------------------------------------------------------------------------------
+ * Errors. Kinds 0..13 keep the reference's values (ogl_beamformer_lib_base.h:10-28).
+ * Kinds 14..16 are this library's additions for failures that only exist in an
+ * in-process CUDA implementation.
+ * ---------------------------------------------------------------------------- */
+typedef enum {
+	BF_LIB_ERR_KIND_NONE                    = 0,
+	BF_LIB_ERR_KIND_VERSION_MISMATCH        = 1,
+	BF_LIB_ERR_KIND_INVALID_ACCESS          = 2,
+	BF_LIB_ERR_KIND_COMPUTE_STAGE_OVERFLOW  = 3,
+	BF_LIB_ERR_KIND_INVALID_COMPUTE_STAGE   = 4,
+	BF_LIB_ERR_KIND_INVALID_START_SHADER    = 5,
+	BF_LIB_ERR_KIND_INVALID_DEMOD_DATA_KIND = 6,
+	BF_LIB_ERR_KIND_INVALID_IMAGE_PLANE     = 7,
+	BF_LIB_ERR_KIND_BUFFER_OVERFLOW         = 8,
+	BF_LIB_ERR_KIND_WORK_QUEUE_FULL         = 9,
+	BF_LIB_ERR_KIND_EXPORT_SPACE_OVERFLOW   = 10,
+	BF_LIB_ERR_KIND_SHARED_MEMORY           = 11,
+	BF_LIB_ERR_KIND_SYNC_VARIABLE           = 12,
+	BF_LIB_ERR_KIND_INVALID_TIMEOUT         = 13,
+	BF_LIB_ERR_KIND_CUDA_DEVICE             = 14, /* no usable CUDA device / context */
+	BF_LIB_ERR_KIND_CUDA_RUNTIME            = 15, /* a CUDA call or kernel launch failed */
+	BF_LIB_ERR_KIND_UNSUPPORTED             = 16, /* stage or DAS mode not implemented here */
+} BeamformerLibErrorKind;
+
+/* Interface version; same number as the reference's shared-memory layout
+ * version (beamformer_work_queue.h:5) so version checks in callers still pass. */
+#define BEAMFORMER_SHARED_MEMORY_VERSION 11u
+
+/* Largest RF push accepted, bytes. The reference bounds pushes by its 2 GB
+ * shared-memory scratch (beamformer_work_queue.h:106-110); the same bound is kept. */
+#define BEAMFORMER_MAX_RF_DATA_SIZE (2147483648ull - 65536ull)
+
+/* ---------------------------- reference interface --------------------------- */
+
+/* ogl_beamformer_lib_base.h:30 / ogl_beamformer_lib.c:127-131 */
+LIB_FN uint32_t beamformer_get_api_version(void);
+
+/* ogl_beamformer_lib_base.h:32-34 / ogl_beamformer_lib.c:133-152 */
+LIB_FN BeamformerLibErrorKind beamformer_get_last_error(void);
+LIB_FN const char *beamformer_get_last_error_string(void);
+LIB_FN const char *beamformer_error_string(BeamformerLibErrorKind kind);
+
+/* Timeout for calls that wait but take no timeout argument. Range [-1, ...);
+ * -1 waits forever, 0 tries once (default).
+ * ogl_beamformer_lib_base.h:36-44 / ogl_beamformer_lib.c:154-164 */
+LIB_FN uint32_t beamformer_set_global_timeout(int32_t timeout_ms);
+
+/* Push RF, beamform, and copy the (complex, 2 floats per point) output volume
+ * into out_data. output_points is clamped to >= 1 and written back.
+ * ogl_beamformer_lib_base.h:46-49 / ogl_beamformer_lib.c:460-491 */
+LIB_FN uint32_t beamform_data_synchronized(void *data, uint32_t data_size, int32_t output_points[3],
+                                           float *out_data, int32_t timeout_ms);
+
+/* Stage timings of the last 32 computes.
+ * ogl_beamformer_lib_base.h:51-52 / ogl_beamformer_lib.c:493-506 */
+LIB_FN uint32_t beamformer_compute_timings(BeamformerComputeStatsTable *output, int32_t timeout_ms);
+
+/* Start a compute on the most recently pushed RF.
+ * ogl_beamformer_lib_base.h:54-55 / ogl_beamformer_lib.c:285-290 */
+LIB_FN uint32_t beamformer_start_compute(void);
+
+/* Wait until previously queued compute has been dispatched.
+ * ogl_beamformer_lib_base.h:57-58 / ogl_beamformer_lib.c:292-300 */
+LIB_FN uint32_t beamformer_wait_for_compute_dispatch(int32_t timeout_ms);
+
+/* ogl_beamformer_lib_base.h:60-65 / ogl_beamformer_lib.c:338-390 */
+LIB_FN uint32_t beamformer_push_data_with_compute(void *data, uint32_t size, uint32_t image_plane_tag);
+LIB_FN uint32_t beamformer_push_data(void *data, uint32_t size);
+LIB_FN uint32_t beamformer_push_channel_mapping(int16_t *mapping,  uint32_t count);
+LIB_FN uint32_t beamformer_push_sparse_elements(int16_t *elements, uint32_t count);
+LIB_FN uint32_t beamformer_push_focal_vectors(float     *vectors,  uint32_t count);
+
+/* ogl_beamformer_lib_base.h:67-71 / ogl_beamformer_lib.c:192-225, 392-429 */
+LIB_FN uint32_t beamformer_set_pipeline_stage_parameters(int32_t stage_index, int32_t parameter);
+LIB_FN uint32_t beamformer_push_pipeline(int32_t *shaders, int32_t shader_count, BeamformerDataKind data_kind);
+LIB_FN uint32_t beamformer_push_parameters(BeamformerParameters *);
+LIB_FN uint32_t beamformer_push_parameters_ui(BeamformerUIParameters *);
+LIB_FN uint32_t beamformer_push_parameters_head(BeamformerParametersHead *);
+
+/* Kaiser low-pass and matched filters into one of BEAMFORMER_FILTER_SLOTS slots.
+ * ogl_beamformer_lib_base.h:73-97 / ogl_beamformer_lib.c:227-254, math.c:125-181 */
+LIB_FN uint32_t beamformer_create_kaiser_low_pass_filter(float beta, float cutoff_frequency,
+                                                         float sampling_frequency,
+                                                         int16_t length, uint8_t slot);
+LIB_FN uint32_t beamformer_create_matched_filter(float xdc_center_frequency, float transmit_frequency,
+                                                 float sampling_frequency,
+                                                 int16_t length, uint8_t slot);
+
+/* ogl_beamformer_lib_base.h:99-103 / ogl_beamformer_lib.c:508-540 */
+LIB_FN int32_t  beamformer_live_parameters_get_dirty_flag(void);
+LIB_FN uint32_t beamformer_set_live_parameters(BeamformerLiveImagingParameters *);
+LIB_FN BeamformerLiveImagingParameters *beamformer_get_live_parameters(void);
+
+/* ------------------------------------------------------------------------------
+ * Extensions of this library (no counterpart in the reference's exported API).
+ * They expose what the reference keeps inside its server process, so that
+ * device-resident callers and tests can reach it.
+ * ---------------------------------------------------------------------------- */
+
+/* Use RF that already lives in device memory for the next compute instead of a
+ * host push: the pipeline reads `device_data` directly (no copy). The caller
+ * keeps the buffer alive and unchanged until that compute has finished.
+ * Counterpart of beamformer_push_data (ogl_beamformer_lib.c:360-382) for a
+ * caller whose data is already on the GPU. */
+LIB_FN uint32_t beamformer_gb300_push_data_device(const void *device_data, uint64_t size);
+
+/* Run computes on this CUDA stream (a cudaStream_t passed as a pointer; NULL
+ * selects the library's own stream). Lets a caller order the pipeline with its
+ * own work and time it with events on the same stream. */
+LIB_FN uint32_t beamformer_gb300_set_stream(void *cuda_stream);
+LIB_FN void    *beamformer_gb300_get_stream(void);
+
+/* Block until every queued compute has finished (timeout_ms as above). */
+LIB_FN uint32_t beamformer_gb300_synchronize(int32_t timeout_ms);
+
+/* Copy a frame out of the device frame store: which = 0 latest beamformed
+ * frame, 1 latest averaged frame (written by the Sum stage). mip_level selects
+ * the Min/Max pyramid level (0 = the frame itself). Output is 2 floats per
+ * point in x-fastest order; out_size is in bytes. The reference keeps these
+ * levels in GL textures (beamformer.c:119-151, 595-607). */
+LIB_FN uint32_t beamformer_gb300_export_frame(uint32_t which, uint32_t mip_level, float *out,
+                                              uint64_t out_size, int32_t dims_out[3]);
+
+/* Copy the output of the last intermediate (non-DAS) stage, i.e. the decoded
+ * or filtered channel data the next stage would read (the reference's
+ * rf_data_ssbos, beamformer.c:153-191). Returns the byte count in *size_out. */
+LIB_FN uint32_t beamformer_gb300_export_channel_data(void *out, uint64_t out_size, uint64_t *size_out);
+
+/* Copy the current filter taps of a slot (as generated on the host, float32). */
+LIB_FN uint32_t beamformer_gb300_get_filter(uint8_t slot, float *taps, int32_t capacity, int32_t *length_out);
+
+/* Number of kernel launches this library issued since load (all streams). */
+LIB_FN uint64_t beamformer_gb300_kernel_launch_count(void);
+
+/* Release all device state (the next call re-initialises it). */
+LIB_FN void     beamformer_gb300_shutdown(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OGL_BEAMFORMER_LIB_H */
