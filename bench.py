@@ -1,0 +1,374 @@
+"""Benchmark: volumes/s of the plain beamforming pipeline on one GB300.
+
+Workload (the 3D configuration): HERCULES on a 128 + 128 element row-column
+array, 128 Hadamard-encoded transmits, 128 receive channels, 2048 int16 samples,
+decode -> demodulate (64-tap Kaiser, decimation 2: 512 complex samples) ->
+cubic DAS to 128 x 128 x 256 voxels -> Sum (16-frame average) -> MinMax.
+One step = 16 consecutive frames pushed and beamformed, i.e. one fully new
+16-frame averaged volume (each compute runs every stage, as the reference does).
+
+value: volumes/s with the 16 RF frames resident in HBM (1.07 GB, larger than L2,
+so no flush is needed), fed through beamformer_gb300_push_data_device +
+beamformer_start_compute, timed with CUDA events on the library's stream.
+e2e: the same through the reference's C ABI from pinned host memory:
+15 x beamformer_push_data_with_compute + beamform_data_synchronized (which
+copies the averaged volume back), host-timed with device syncs on both sides.
+
+--impl reference times the reference path's CPU restatement (the oracle; the
+reference's own code is GLSL and cannot run here) on the host cores, on a
+bounded voxel/channel sample of the same workload scaled to volumes/s.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FRAMES = 16
+POINTS = (128, 128, 256)
+S, C, T = 2048, 128, 128
+FILTER_TAPS = 64
+N_POINTS, N_SPECKLE = 200, 20000
+METRIC = "volumes/s plain vs mixed-precision/learned pipeline at NRMSE <= -40 dB, 1 GB300"
+DAS_FLOPS_PER_TERM = 40            # cubic sample-op: interpolation, apodization, phase rotation, accumulate
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--speckle", type=int, default=N_SPECKLE)
+    return ap.parse_args()
+
+
+def workload():
+    from ogl_beamforming_cuda_gb300 import synth
+    bp = synth.make_parameters(samples=S, channels=C, transmits=T, points=POINTS, decimation=2, f_number=1.0,
+                               interpolate=1, frames=FRAMES, filter_length=FILTER_TAPS)
+    return bp, synth.default_pipeline(sum_and_minmax=True), synth.kaiser_spec(FILTER_TAPS)
+
+
+def config_dict(extra=None):
+    d = {"workload": "HERCULES RCA 128+128, 128 tx, 2048 samples int16 -> decode -> demod(64 taps, /4) -> "
+                     "cubic DAS 128x128x256 -> 16-frame sum -> min_max",
+         "frames_per_volume": FRAMES, "voxels": int(np.prod(POINTS)), "transmits": T, "channels": C,
+         "samples": S, "interpolation": "cubic", "scatterers": N_POINTS, "speckle_scatterers": N_SPECKLE,
+         "l2": "inputs larger than L2 (16 frames x 67 MB resident), no flush", "parallelism": "replicas"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+def frames_on_device(bp, device, seed0=1000, speckle=N_SPECKLE):
+    """16 consecutive frames of one static scatterer field: decoded traces computed
+    once, each frame re-encoded with its own noise realisation."""
+    import torch
+    from ogl_beamforming_cuda_gb300 import synth
+    pos, amp = synth.scatterers(seed0, N_POINTS, speckle)
+    x = synth.decoded_traces(bp, pos, amp, device=device, batch=64)
+    out = torch.empty((FRAMES, C, T, S), dtype=torch.int16, device=device)
+    for f in range(FRAMES):
+        out[f] = synth.encode_and_quantise(x, seed0 + f)
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+def stage_times(bf, rows):
+    """Mean per-stage seconds over the last `rows` computes from the library's timing table."""
+    from ogl_beamforming_cuda_gb300 import abi
+    times, _ = bf.timings()
+    nz = times[np.any(times > 0, axis=1)]
+    nz = nz[-rows:] if len(nz) > rows else nz
+    names = {v: k for k, v in abi.SHADER.items()}
+    return {names[i]: float(nz[:, i].mean()) for i in range(nz.shape[1]) if i in names and np.any(nz[:, i] > 0)}
+
+
+def algorithmic_bytes():
+    Sp = S // 4
+    vox = int(np.prod(POINTS))
+    return {
+        "DecodeInt16ToFloat": S * C * T * (2 + 4),
+        "DemodulateFloat": S * C * T * 4 + Sp * C * T * 8,
+        "Sum": (FRAMES + 1) * vox * 8,
+        "MinMax": vox * 8 + vox * 8 // 8,
+    }
+
+
+def fp32_peak_tflops(peaks):
+    """Nominal FP32 FMA throughput: 152 SMs x 128 lanes x 2 flops x max SM clock.
+    MEASURED_PEAKS.json carries no FP32 figure, so the measured max clock is used."""
+    mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    return 152 * 128 * 2 * mhz * 1e6 / 1e12
+
+
+def run_ours(args, rank, world, local, dist):
+    import torch
+    torch.cuda.set_device(local)
+    from ogl_beamforming_cuda_gb300.client import Beamformer
+    bp, pipe, kaiser = workload()
+    bf = Beamformer().configure(bp, pipe, kaiser=kaiser)
+    frames = frames_on_device(bp, f"cuda:{local}", speckle=args.speckle)
+    nbytes = frames[0].numel() * 2
+    stream = torch.cuda.ExternalStream(bf.lib.beamformer_gb300_get_stream())
+
+    def step():
+        for f in range(FRAMES):
+            bf.push_device(frames[f].data_ptr(), nbytes)
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    bf.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    l0 = bf.launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        bf.synchronize()
+        torch.cuda.synchronize()
+    barrier()
+    launches = bf.launches() - l0
+    t = e0.elapsed_time(e1) / 1e3
+    stages = stage_times(bf, 32)
+
+    # end to end through the reference's C ABI, pinned host RF in, averaged volume out
+    host = frames.cpu().pin_memory()
+    del frames
+    vox = int(np.prod(POINTS))
+    out = torch.empty(2 * vox, dtype=torch.float32).pin_memory()
+    pts = (ctypes.c_int32 * 3)(*POINTS)
+    L = bf.lib
+    L.beamformer_set_global_timeout(-1)      # block on a busy RF slot, as a streaming client does
+
+    def e2e_step():
+        for f in range(FRAMES - 1):
+            assert L.beamformer_push_data_with_compute(ctypes.c_void_p(host[f].data_ptr()), nbytes, 0)
+        assert L.beamform_data_synchronized(ctypes.c_void_p(host[FRAMES - 1].data_ptr()), nbytes, pts,
+                                            ctypes.cast(out.data_ptr(), ctypes.POINTER(ctypes.c_float)), -1)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    h0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    te = time.perf_counter() - h0
+    barrier()
+    if dist:
+        tt = torch.tensor([t, te], device=f"cuda:{local}")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t, te = float(tt[0]), float(tt[1])
+    return dict(t=t, te=te, stages=stages, launches=launches, clocks=clk.summary(), nbytes=nbytes, out_bytes=8 * vox)
+
+
+def cpu_sample(budget_s=12.0):
+    """Volumes/s of the CPU oracle (reference semantics, all host cores), estimated
+    from a bounded sample: decode and demodulation of 4 of the 128 channels, DAS
+    of voxel ranges spread over the volume, and the full sum and min/max; each
+    part scaled to a full 16-frame volume."""
+    from oracle import bf_oracle as O
+    from ogl_beamforming_cuda_gb300 import synth
+    threads = O.threads()
+    bp, pipe, kaiser = workload()
+    csub = 4
+    sub = synth.make_parameters(samples=S, channels=csub, transmits=T, points=POINTS, decimation=2, interpolate=1,
+                                frames=FRAMES)
+    rng = np.random.default_rng(0)
+    raw = rng.integers(-16384, 16384, size=(csub, T, S), dtype=np.int16)
+    orc = O.OraclePipeline()
+    orc.bp, orc.shaders = sub, [pipe[0], pipe[1]]
+    orc.create_kaiser(*kaiser, 0)
+    t0 = time.perf_counter()
+    orc.compute(raw)
+    t_front = (time.perf_counter() - t0) * (C / csub)
+
+    plan = O.plan(bp, pipe, [0] * len(pipe), 0, [(0, kaiser[3], kaiser[2], kaiser[0], kaiser[1]), None, None, None])
+    rf = np.zeros(2 * (S // 4) * C * T, np.float32)
+    focal = np.zeros(512, np.float32)
+    focal[1::2] = np.inf
+    sparse = np.arange(256, dtype=np.int16)
+    V = int(np.prod(POINTS))
+    frame = np.zeros(2 * V, np.float32)
+    ranges = 16
+    per = 64
+    t0 = time.perf_counter()
+    for i in range(ranges):
+        v0 = (V // ranges) * i + V // (2 * ranges)
+        O.das(plan.das, rf, POINTS, sparse, focal, fast=True, voxel_begin=v0, voxel_end=v0 + per, out=frame)
+    probe = time.perf_counter() - t0
+    per = int(max(64, min(V // ranges, per * (0.6 * budget_s) / max(probe, 1e-3))))
+    t0 = time.perf_counter()
+    for i in range(ranges):
+        v0 = (V // ranges) * i + V // (2 * ranges) - per // 2
+        O.das(plan.das, rf, POINTS, sparse, focal, fast=True, voxel_begin=v0, voxel_end=v0 + per, out=frame)
+    t_das = (time.perf_counter() - t0) * V / (ranges * per)
+
+    frames = [np.zeros(2 * V, np.float32) for _ in range(FRAMES)]
+    t0 = time.perf_counter()
+    O.sum_frames(frames, np.float32(1 / FRAMES), POINTS)
+    O.min_max(frames[0], POINTS)
+    t_tail = time.perf_counter() - t0
+    t_volume = FRAMES * (t_front + t_das + t_tail)
+    sample = (f"decode+demod of {csub}/{C} channels, DAS of {ranges * per}/{V} voxels in {ranges} ranges, "
+              f"full sum+min_max; scaled to {FRAMES} frames (extrapolated)")
+    return {"value": 1.0 / t_volume, "unit": "volumes/s", "cores": threads, "kind": "port", "sample": sample,
+            "seconds_per_volume": t_volume}
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    peaks = measured_peaks()
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        samples = []
+        for _ in range(max(args.warmup, 0)):
+            cpu_sample(budget_s=2.0)
+        for _ in range(max(args.steps, 1)):
+            samples.append(cpu_sample(budget_s=3.0))
+        v = statistics.median(s["value"] for s in samples)
+        cb = dict(samples[0])
+        cb["value"] = v
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": v, "unit": "volumes/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_dict({"reference_arm": "CPU restatement of the reference shaders (oracle); the "
+                                   "reference's GLSL path needs an OpenGL context, unavailable on this box"}),
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "volumes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return 0
+
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+        dist = tdist
+    r = run_ours(args, rank, world, local, dist)
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+    value = args.steps * world / r["t"]
+    e2e = args.steps * world / r["te"]
+    st = r["stages"]
+    das_t = st.get("DASFast") or st.get("DAS")
+    V = int(np.prod(POINTS))
+    flops = V * T * C * DAS_FLOPS_PER_TERM
+    peak = fp32_peak_tflops(peaks)
+    achieved = flops / das_t / 1e12 if das_t else None
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    stage_roof = {}
+    for k, b in algorithmic_bytes().items():
+        if st.get(k):
+            gbs = b / st[k] / 1e9
+            stage_roof[k] = {"ms": st[k] * 1e3, "bytes": b, "GB/s": gbs, "frac_of_measured_hbm": gbs / hbm}
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "das_traffic.json")
+    if os.path.exists(tfile):
+        traffic = json.load(open(tfile)).get("dram_bytes_per_launch")
+    line = {
+        "metric": METRIC, "value": value, "unit": "volumes/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["t"] / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded RF generator)",
+        "config": config_dict(),
+        "e2e": {"value": e2e, "unit": "volumes/s", "h2d_bytes_per_step": FRAMES * r["nbytes"],
+                "d2h_bytes_per_step": r["out_bytes"]},
+        "gpu_launches": r["launches"],
+        "roofline": {"kernel": "das_kernel<HERCULES, cubic, fast>", "bound": "fp32", "achieved": achieved,
+                     "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
+                     "traffic": traffic, "algorithmic_flops_per_launch": flops,
+                     "peak_source": "nominal FP32 (152 SMs x 128 lanes x 2 x sm_max_mhz of MEASURED_PEAKS.json)",
+                     "das_ms": das_t * 1e3 if das_t else None},
+        "stages": stage_roof,
+        "clocks": r["clocks"],
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_sample()
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -324,6 +324,11 @@ LIB_FN uint32_t beamformer_gb300_export_channel_data(void *out, uint64_t out_siz
 /* Copy the current filter taps of a slot (as generated on the host, float32). */
 LIB_FN uint32_t beamformer_gb300_get_filter(uint8_t slot, float *taps, int32_t capacity, int32_t *length_out);
 
+/* Interpolation used by the DAS stage: -1 follows BeamformerParameters.interpolate
+ * (0 nearest, non-zero cubic, das.glsl:64-72); 0 nearest, 1 cubic, 2 linear.
+ * Linear interpolation has no counterpart in the reference. */
+LIB_FN uint32_t beamformer_gb300_set_interpolation(int32_t mode);
+
 /* Number of kernel launches this library issued since load (all streams). */
 LIB_FN uint64_t beamformer_gb300_kernel_launch_count(void);
 

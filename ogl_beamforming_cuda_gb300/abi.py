@@ -98,6 +98,7 @@ SIGNATURES = [
     ("beamformer_gb300_export_frame", u32, [u32, u32, P(f32), ctypes.c_uint64, P(i32)]),
     ("beamformer_gb300_export_channel_data", u32, [vp, ctypes.c_uint64, P(ctypes.c_uint64)]),
     ("beamformer_gb300_get_filter", u32, [ctypes.c_uint8, P(f32), i32, P(i32)]),
+    ("beamformer_gb300_set_interpolation", u32, [i32]),
     ("beamformer_gb300_kernel_launch_count", ctypes.c_uint64, []),
     ("beamformer_gb300_shutdown", None, []),
 ]

@@ -1,0 +1,112 @@
+/*
+ * bf_kernels.h -- launch interface between the host library (bf_library.cpp)
+ * and the sm_103a kernels (bf_decode.cu, bf_filter.cu, bf_das.cu,
+ * bf_reduce.cu). Plain structs passed by value to the kernels.
+ */
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace bf {
+
+/* Strides in elements of the stage's storage type, as the reference's stage
+ * uniform blocks define them (beamformer.h:112-147). */
+struct Strides {
+	uint32_t in_channel, in_sample, in_transmit;
+	uint32_t out_channel, out_sample, out_transmit;
+};
+
+/* ------------------------------- decode ---------------------------------- */
+enum DecodeInput  { DEC_IN_I16 = 0, DEC_IN_I16C = 1, DEC_IN_F32 = 2, DEC_IN_F32C = 3 };
+enum DecodeOutput { DEC_OUT_COMPLEX = 0, DEC_OUT_REAL_PAIRS = 1 };
+
+struct DecodeParams {
+	const void    *in;             /* raw RF or previous stage output */
+	uint64_t       in_elems;       /* element count of `in` (bounds) */
+	float         *out;            /* float2 output */
+	uint64_t       out_vec2;       /* float2 count of `out` (bounds) */
+	const int16_t *channel_map;    /* device, 256 entries; null = identity */
+	const int8_t  *hadamard;       /* device, T*T, row = transmit */
+	Strides        st;
+	uint32_t       samples;        /* samples per transmit row to produce */
+	uint32_t       in_limit;       /* samples at or beyond this read as zero (the reference's gather guard) */
+	uint32_t       channels;
+	uint32_t       transmits;      /* Hadamard order */
+	uint32_t       sylvester;      /* Sylvester factor (power of two) */
+	uint32_t       base;           /* 1, 12 or 20: dense factor of the Kronecker product */
+	uint32_t       hadamard_mode;  /* 0 none (reshape), 1 Hadamard */
+	uint32_t       first_stage;    /* map channels and read raw layout */
+	int            input;          /* DecodeInput */
+	int            output;         /* DecodeOutput */
+};
+
+/* --------------------------- demodulate / filter ------------------------- */
+enum FilterKind { FILT_DEMOD_F32 = 0, FILT_DEMOD_I16 = 1, FILT_COMPLEX = 2 };
+
+struct FilterParams {
+	const void    *in;
+	uint64_t       in_elems;
+	void          *out;
+	uint64_t       out_elems;
+	const float   *taps;           /* device, reversed per phase (see bf_filter.cu) */
+	const float2  *phasor;         /* device, per input index: (cos, sin) of the demodulation angle */
+	const int16_t *channel_map;
+	Strides        st;
+	uint32_t       out_samples;    /* outputs per row (target) */
+	uint32_t       in_samples;     /* inputs per row usable (target * decimation) */
+	uint32_t       channels, transmits;
+	uint32_t       decimation;
+	uint32_t       taps_len;
+	uint32_t       map_channels;
+	int            kind;
+};
+
+/* ---------------------------------- DAS ---------------------------------- */
+enum DasFamily { DAS_FORCES = 0, DAS_HERCULES = 1, DAS_RCA = 2, DAS_NONE = 3 };
+enum DasInterp { INTERP_NEAREST = 0, INTERP_CUBIC = 1, INTERP_LINEAR = 2 };
+
+struct DasParams {
+	const float2  *rf;
+	int64_t        rf_count;       /* float2 samples readable (bound range of the reference) */
+	float2        *frame;
+	int32_t        dims[3];
+	float          M[16];          /* voxel -> world, column major */
+	float          X[16];          /* world -> transducer (xdc_transform) */
+	int32_t        S, C, T;        /* dec_data_dim */
+	int32_t        family, das_id, interp, fast, coherency, sparse_mode;
+	int32_t        tx_rows, rx_cols, rx_rows, loop_end;
+	float          fs, fc, c, toff;
+	float          r360_fc;        /* radians(360) * center_frequency */
+	float          apod_scale;     /* f_number * radians(180) */
+	float          apod_hi;        /* 0.25 * radians(360) */
+	float          inv_sqrt_T;
+	float          px, py;
+	float          cy_forces;      /* pitch.y * floor(channels / 2) */
+	const float4  *focal;          /* per focal vector: sin(angle), cos(angle), depth, isinf(depth) */
+	const int16_t *sparse;
+	/* division by the constants c and fs: x * (1/b) corrected by one FMA, used only
+	 * where a device-side exhaustive check proved it equal to IEEE division */
+	float          rc, rfs;
+	float          c_lo, c_hi, fs_lo, fs_hi;   /* verified ranges of x (empty: always IEEE) */
+	/* split of the outer (receive channel / transmit) loop over groups of blocks;
+	 * groups > 1 writes partial sums to `partial` (groups x voxels) */
+	int32_t        groups, per_group;
+	float2        *partial;
+};
+
+/* Exhaustively compare x * rb + correction with IEEE x / b for every float x in
+ * [lo, hi]; *mismatch receives the count of differing x. */
+cudaError_t launch_verify_division(float b, float rb, float lo, float hi, unsigned long long *mismatch, cudaStream_t s);
+
+/* launchers: return cudaSuccess or the launch error */
+cudaError_t launch_decode(const DecodeParams &p, cudaStream_t s);
+cudaError_t launch_filter(const FilterParams &p, cudaStream_t s);
+cudaError_t launch_das(const DasParams &p, cudaStream_t s);
+cudaError_t launch_sum(float2 *out, const float2 *const *ins, int count, float prescale, const int32_t dims[3],
+                       cudaStream_t s);
+cudaError_t launch_min_max(const float2 *level0, const int32_t dims[3], int mips, float2 *levels, cudaStream_t s);
+
+/* kernel launches issued since load (all launchers count here) */
+extern uint64_t g_kernel_launches;
+
+} /* namespace bf */

@@ -1,0 +1,1066 @@
+/*
+ * bf_library.cpp -- the C ABI of include/ogl_beamformer_lib.h.
+ *
+ * In-process replacement of the reference's client library
+ * (helpers/ogl_beamformer_lib.c) together with the compute side of its server
+ * (beamformer.c: complete_queue :842-1111, do_compute_shader :521-709,
+ * beamformer_rf_upload :1230-1276, coalesce_timing_table :1113-1173).
+ *
+ * Data flow of one compute on the GPU:
+ *   RF push (host -> device, upload stream, 3-slot ring as the reference's
+ *   MAX_RAW_DATA_FRAMES_IN_FLIGHT) -> compute stream waits on the upload event
+ *   -> planned stages (decode, demodulate/filter, DAS, sum, min/max) on two
+ *   ping-pong channel buffers and a 16-frame ring -> events per stage feed the
+ *   timing table.
+ *
+ * Error behaviour follows the reference: every entry point returns 1/0 (or a
+ * pointer/-1) and sets a process-global last error. Validation that needs no
+ * device (pipeline, sizes, timeouts) runs before any CUDA call, as the
+ * reference validates before touching shared memory.
+ */
+#include "ogl_beamformer_lib.h"
+#include "bf_host.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+using namespace bf;
+
+namespace {
+
+constexpr int RF_SLOTS = 3;                 /* MAX_RAW_DATA_FRAMES_IN_FLIGHT (beamformer.h:180) */
+constexpr int TIMING_SLOTS = 8;
+constexpr uint64_t SCRATCH_SIZE = BEAMFORMER_MAX_RF_DATA_SIZE;
+
+struct DeviceFrame {
+	float2  *data = nullptr;
+	float2  *levels = nullptr;
+	int32_t  dims[3] = {0, 0, 0};
+	int32_t  mips = 0;
+	uint64_t level_texels = 0;
+	bool     written = false;
+};
+
+struct PendingTiming {
+	cudaEvent_t ev[MAX_COMPUTE_SHADER_STAGES + 1] = {};
+	int32_t     shaders[MAX_COMPUTE_SHADER_STAGES] = {};
+	int32_t     count = 0;
+	bool        active = false;
+};
+
+struct StageTables {
+	float   *taps = nullptr;     /* polyphase-arranged taps */
+	size_t   taps_cap = 0;
+	float2  *phasor = nullptr;   /* demodulation phasor per input index */
+	size_t   phasor_cap = 0;
+};
+
+struct Context {
+	/* ---- state pushed by the caller ---- */
+	BeamformerParameters params{};
+	int32_t  shaders[MAX_COMPUTE_SHADER_STAGES] = {};
+	uint8_t  slots[MAX_COMPUTE_SHADER_STAGES] = {};
+	int32_t  shader_count = 0;
+	int32_t  data_kind = BeamformerDataKind_Int16;
+	int16_t  channel_mapping[256];
+	int16_t  sparse_elements[256];
+	float    focal_vectors[512] = {};
+	FilterSpec filters[BEAMFORMER_FILTER_SLOTS];
+	std::vector<float> taps[BEAMFORMER_FILTER_SLOTS];
+	BeamformerLiveImagingParameters live{};
+	uint32_t live_dirty = 0;
+	int32_t  timeout_ms = 0;
+	BeamformerLibErrorKind last_error = BF_LIB_ERR_KIND_NONE;
+	bool     dirty = true;
+
+	/* ---- device ---- */
+	bool         ready = false;
+	cudaStream_t own_stream = nullptr, stream = nullptr, upload_stream = nullptr;
+	void        *raw[RF_SLOTS] = {};
+	uint64_t     raw_cap = 0, raw_size[RF_SLOTS] = {};
+	cudaEvent_t  upload_done[RF_SLOTS] = {}, compute_done[RF_SLOTS] = {};
+	bool         slot_used[RF_SLOTS] = {};
+	uint32_t     insert_index = 0;
+	int          latest_slot = -1;
+	const void  *ext_rf = nullptr;
+	uint64_t     ext_size = 0;
+	bool         use_ext = false;
+	cudaEvent_t  ext_done = nullptr, last_done = nullptr;
+
+	float2      *chan[2] = {};
+	uint64_t     chan_bytes = 0;
+	int          last_chan = -1;
+
+	int8_t      *hadamard = nullptr;
+	int32_t      hadamard_order = 0, hadamard_sylvester = 0, hadamard_base = 0;
+	bool         hadamard_ok = false;
+	int16_t     *d_chmap = nullptr, *d_sparse = nullptr;
+	float4      *d_focal = nullptr;
+	StageTables  stage_tables[MAX_COMPUTE_SHADER_STAGES];
+
+	Plan         plan{};
+	bool         plan_ok = false;
+	float        M[16] = {};
+
+	DeviceFrame  frames[MAX_BEAMFORMED_SAVED_FRAMES];
+	DeviceFrame  averaged[2];
+	uint32_t     frame_counter = 0, averaged_counter = 0;
+	int          latest_kind = -1, latest_index = -1;   /* 0 frame ring, 1 averaged */
+	int          latest_das_index = -1;
+
+	PendingTiming timing[TIMING_SLOTS];
+	uint32_t     timing_next = 0;
+	BeamformerComputeStatsTable stats{};
+	uint32_t     stats_index = 0, rf_delta_index = 0;
+	std::chrono::steady_clock::time_point last_upload{};
+	bool         have_last_upload = false;
+	int32_t      interpolation_override = -1;
+
+	/* DAS: partial sums of channel groups, and verified division ranges per divisor */
+	float2      *das_partial = nullptr;
+	uint64_t     das_partial_bytes = 0;
+	unsigned long long *d_mismatch = nullptr;
+	struct DivCheck { float b, lo, hi; };
+	std::vector<DivCheck> div_checks;
+
+	Context()
+	{
+		for (int i = 0; i < 256; i++) { channel_mapping[i] = (int16_t)i; sparse_elements[i] = (int16_t)i; }
+	}
+};
+
+Context g;
+
+uint32_t fail(BeamformerLibErrorKind k)
+{
+	g.last_error = k;
+	return 0;
+}
+
+bool cuda_ok(cudaError_t e)
+{
+	if (e != cudaSuccess) {
+		g.last_error = BF_LIB_ERR_KIND_CUDA_RUNTIME;
+		cudaGetLastError();
+		return false;
+	}
+	return true;
+}
+
+/* Wait for an event with the reference's timeout convention: -1 forever,
+ * 0 one try, N milliseconds. */
+bool wait_event(cudaEvent_t ev, int32_t timeout_ms)
+{
+	if (!ev) return true;
+	if (timeout_ms < 0) return cudaEventSynchronize(ev) == cudaSuccess;
+	auto start = std::chrono::steady_clock::now();
+	for (;;) {
+		cudaError_t e = cudaEventQuery(ev);
+		if (e == cudaSuccess) return true;
+		if (e != cudaErrorNotReady) { cudaGetLastError(); return false; }
+		auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - start).count();
+		if (ms >= timeout_ms) return false;
+		std::this_thread::sleep_for(std::chrono::microseconds(50));
+	}
+}
+
+bool ensure_cuda()
+{
+	if (g.ready) return true;
+	int n = 0;
+	if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+		cudaGetLastError();
+		return fail(BF_LIB_ERR_KIND_CUDA_DEVICE), false;
+	}
+	if (!cuda_ok(cudaStreamCreateWithFlags(&g.own_stream, cudaStreamNonBlocking))) return false;
+	if (!cuda_ok(cudaStreamCreateWithFlags(&g.upload_stream, cudaStreamNonBlocking))) return false;
+	for (int i = 0; i < RF_SLOTS; i++) {
+		if (!cuda_ok(cudaEventCreateWithFlags(&g.upload_done[i], cudaEventDisableTiming))) return false;
+		if (!cuda_ok(cudaEventCreateWithFlags(&g.compute_done[i], cudaEventDisableTiming))) return false;
+	}
+	if (!cuda_ok(cudaEventCreateWithFlags(&g.ext_done, cudaEventDisableTiming))) return false;
+	for (auto &t : g.timing)
+		for (auto &e : t.ev)
+			if (!cuda_ok(cudaEventCreate(&e))) return false;
+	if (!cuda_ok(cudaMalloc(&g.d_chmap, 256 * sizeof(int16_t)))) return false;
+	if (!cuda_ok(cudaMalloc(&g.d_sparse, 256 * sizeof(int16_t)))) return false;
+	if (!cuda_ok(cudaMalloc(&g.d_focal, 256 * sizeof(float4)))) return false;
+	if (!g.stream) g.stream = g.own_stream;
+	g.ready = true;
+	g.dirty = true;
+	return true;
+}
+
+void free_frame(DeviceFrame &f)
+{
+	cudaFree(f.data);
+	cudaFree(f.levels);
+	f = DeviceFrame{};
+}
+
+bool ensure_frame(DeviceFrame &f, const int32_t dims[3])
+{
+	if (f.data && f.dims[0] == dims[0] && f.dims[1] == dims[1] && f.dims[2] == dims[2]) return true;
+	free_frame(f);
+	uint64_t n = (uint64_t)dims[0] * dims[1] * dims[2];
+	f.mips = frame_mips(dims);
+	f.level_texels = 0;
+	for (int l = 1; l < f.mips; l++) {
+		uint64_t x = (uint64_t)dims[0] >> l, y = (uint64_t)dims[1] >> l, z = (uint64_t)dims[2] >> l;
+		f.level_texels += (x ? x : 1) * (y ? y : 1) * (z ? z : 1);
+	}
+	if (!cuda_ok(cudaMalloc(&f.data, n * sizeof(float2)))) return false;
+	if (f.level_texels && !cuda_ok(cudaMalloc(&f.levels, f.level_texels * sizeof(float2)))) return false;
+	cudaMemsetAsync(f.data, 0, n * sizeof(float2), g.stream);
+	std::memcpy(f.dims, dims, sizeof(f.dims));
+	f.written = false;
+	return true;
+}
+
+/* (Re)build everything derived from the pushed state. */
+bool prepare()
+{
+	if (!g.dirty && g.plan_ok) return true;
+	g.plan_ok = false;
+	plan_pipeline(g.params, g.shaders, g.slots, g.shader_count, g.data_kind, g.filters, g.plan);
+	const Plan &pl = g.plan;
+
+	for (int i = 0; i < pl.count; i++) {
+		int k = pl.shaders[i];
+		if (k == BeamformerShaderKind_CudaHilbert || k == BeamformerShaderKind_Render3D)
+			return fail(BF_LIB_ERR_KIND_UNSUPPORTED), false;
+		if (k == BeamformerShaderKind_Demodulate || k == BeamformerShaderKind_DemodulateFloat ||
+		    k == BeamformerShaderKind_Filter) {
+			const FilterSpec &f = g.filters[pl.slots[i] % BEAMFORMER_FILTER_SLOTS];
+			if (f.kind < 0 || f.length <= 0) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS), false;
+		}
+	}
+
+	/* channel buffers: 2 * 4 * samples * channels * transmits (beamformer.c:165) */
+	uint64_t need = 8ull * g.params.dec_data_dim[0] * g.params.dec_data_dim[1] * g.params.dec_data_dim[2];
+	if (need > g.chan_bytes) {
+		cudaStreamSynchronize(g.stream);
+		cudaFree(g.chan[0]); cudaFree(g.chan[1]);
+		g.chan[0] = g.chan[1] = nullptr;
+		g.chan_bytes = 0;
+		if (!cuda_ok(cudaMalloc(&g.chan[0], need)) || !cuda_ok(cudaMalloc(&g.chan[1], need))) return false;
+		cudaMemsetAsync(g.chan[0], 0, need, g.stream);
+		cudaMemsetAsync(g.chan[1], 0, need, g.stream);
+		g.chan_bytes = need;
+	}
+	/* a new plan may write only part of a channel buffer (the reference's dispatch
+	 * grid decides); start it from zeros rather than the previous plan's data */
+	cudaMemsetAsync(g.chan[0], 0, g.chan_bytes, g.stream);
+	cudaMemsetAsync(g.chan[1], 0, g.chan_bytes, g.stream);
+
+	/* Hadamard matrix for the transmit count (uploaded as the reference does when dims change) */
+	int32_t order = (int32_t)g.params.dec_data_dim[2];
+	if (order != g.hadamard_order) {
+		std::vector<int8_t> h;
+		g.hadamard_ok = hadamard_matrix(order, h, g.hadamard_sylvester, g.hadamard_base);
+		cudaStreamSynchronize(g.stream);
+		cudaFree(g.hadamard);
+		g.hadamard = nullptr;
+		if (g.hadamard_ok) {
+			if (!cuda_ok(cudaMalloc(&g.hadamard, h.size()))) return false;
+			if (!cuda_ok(cudaMemcpy(g.hadamard, h.data(), h.size(), cudaMemcpyHostToDevice))) return false;
+		}
+		g.hadamard_order = order;
+	}
+	bool uses_decode = false;
+	for (int i = 0; i < pl.count; i++)
+		if (pl.shaders[i] == BeamformerShaderKind_Decode || pl.shaders[i] == BeamformerShaderKind_DecodeInt16Complex ||
+		    pl.shaders[i] == BeamformerShaderKind_DecodeFloat || pl.shaders[i] == BeamformerShaderKind_DecodeFloatComplex ||
+		    pl.shaders[i] == BeamformerShaderKind_DecodeInt16ToFloat || pl.shaders[i] == BeamformerShaderKind_CudaDecode)
+			uses_decode = true;
+	if (uses_decode && pl.decode_mode == DECODE_MODE_HADAMARD && !g.hadamard_ok)
+		return fail(BF_LIB_ERR_KIND_UNSUPPORTED), false;
+
+	/* per-stage filter taps (polyphase arranged) and demodulation phasors */
+	for (int i = 0; i < pl.count; i++) {
+		int k = pl.shaders[i];
+		if (k != BeamformerShaderKind_Demodulate && k != BeamformerShaderKind_DemodulateFloat &&
+		    k != BeamformerShaderKind_Filter)
+			continue;
+		const bool is_filter = k == BeamformerShaderKind_Filter;
+		const std::vector<float> &h = g.taps[pl.slots[i] % BEAMFORMER_FILTER_SLOTS];
+		const uint32_t L = (uint32_t)h.size();
+		const uint32_t D = is_filter ? 1 : pl.demod_decimation;
+		const uint32_t Lp = (L + D - 1) / D, Lpad = Lp * D;
+		std::vector<float> hp((size_t)D * Lp, 0.0f);
+		for (uint32_t kp = Lpad - L; kp < Lpad; kp++) hp[(size_t)(kp % D) * Lp + kp / D] = h[Lpad - 1 - kp];
+		StageTables &st = g.stage_tables[i];
+		if (hp.size() > st.taps_cap) {
+			cudaFree(st.taps);
+			st.taps = nullptr;
+			if (!cuda_ok(cudaMalloc(&st.taps, hp.size() * sizeof(float)))) return false;
+			st.taps_cap = hp.size();
+		}
+		if (!cuda_ok(cudaMemcpyAsync(st.taps, hp.data(), hp.size() * sizeof(float), cudaMemcpyHostToDevice, g.stream)))
+			return false;
+		cudaStreamSynchronize(g.stream);
+		if (!is_filter) {
+			const bool map = pl.demod_map != 0;
+			const uint32_t target = map ? pl.demod_st.out_channel / pl.demod_st.out_sample : pl.demod_st.out_transmit;
+			const uint32_t n_in = target * D;
+			std::vector<float2> ph(n_in);
+			const float r360 = 360.0f * DEG2RAD_F;
+			for (uint32_t j = 0; j < n_in; j++) {
+				/* filter.glsl rotate_iq(v, -j): radians(360) * f * index / fs */
+				float arg = r360 * pl.demod_frequency * (float)(-(int32_t)j) / pl.demod_fs;
+				ph[j] = make_float2(cosf(arg), sinf(arg));
+			}
+			if (n_in > st.phasor_cap) {
+				cudaFree(st.phasor);
+				st.phasor = nullptr;
+				if (!cuda_ok(cudaMalloc(&st.phasor, n_in * sizeof(float2)))) return false;
+				st.phasor_cap = n_in;
+			}
+			if (n_in && !cuda_ok(cudaMemcpy(st.phasor, ph.data(), n_in * sizeof(float2), cudaMemcpyHostToDevice)))
+				return false;
+		}
+	}
+
+	/* channel mapping, sparse elements, focal vectors (sin/cos of the angle on the host) */
+	float4 focal[256];
+	for (int i = 0; i < 256; i++) {
+		float angle = g.focal_vectors[2 * i] * DEG2RAD_F;
+		float depth = g.focal_vectors[2 * i + 1];
+		focal[i] = make_float4(sinf(angle), cosf(angle), depth, std::isinf(depth) ? 1.0f : 0.0f);
+	}
+	if (!cuda_ok(cudaMemcpy(g.d_chmap, g.channel_mapping, sizeof(g.channel_mapping), cudaMemcpyHostToDevice))) return false;
+	if (!cuda_ok(cudaMemcpy(g.d_sparse, g.sparse_elements, sizeof(g.sparse_elements), cudaMemcpyHostToDevice))) return false;
+	if (!cuda_ok(cudaMemcpy(g.d_focal, focal, sizeof(focal), cudaMemcpyHostToDevice))) return false;
+
+	voxel_transform(pl.das, g.M);
+	g.plan_ok = true;
+	g.dirty = false;
+	return true;
+}
+
+
+/* Range of dividends for which the reciprocal division by b is exact (checked
+ * once per divisor on the device); an empty range (lo > hi) means IEEE division. */
+bool division_range(float b, float lo, float hi, float &out_lo, float &out_hi)
+{
+	for (const auto &d : g.div_checks)
+		if (d.b == b && d.lo <= lo) { out_lo = d.lo; out_hi = d.hi; return true; }
+	out_lo = INFINITY; out_hi = 0.0f;
+	if (!(b > 0.0f) || !std::isfinite(b)) return true;
+	if (!g.d_mismatch && !cuda_ok(cudaMalloc(&g.d_mismatch, sizeof(unsigned long long)))) return false;
+	unsigned long long bad = 0;
+	if (!cuda_ok(cudaMemsetAsync(g.d_mismatch, 0, sizeof(bad), g.stream))) return false;
+	if (!cuda_ok(launch_verify_division(b, 1.0f / b, lo, hi, g.d_mismatch, g.stream))) return false;
+	if (!cuda_ok(cudaMemcpyAsync(&bad, g.d_mismatch, sizeof(bad), cudaMemcpyDeviceToHost, g.stream))) return false;
+	if (!cuda_ok(cudaStreamSynchronize(g.stream))) return false;
+	if (bad == 0) { out_lo = lo; out_hi = hi; }
+	g.div_checks.push_back({b, out_lo, out_hi});
+	return true;
+}
+
+bool ensure_raw_capacity(uint64_t size)
+{
+	if (size <= g.raw_cap) return true;
+	for (int i = 0; i < RF_SLOTS; i++)
+		if (g.slot_used[i]) cudaEventSynchronize(g.compute_done[i]);
+	cudaStreamSynchronize(g.upload_stream);
+	uint64_t cap = (size + (2ull << 20) - 1) & ~((2ull << 20) - 1);
+	for (int i = 0; i < RF_SLOTS; i++) {
+		cudaFree(g.raw[i]);
+		g.raw[i] = nullptr;
+	}
+	g.raw_cap = 0;
+	for (int i = 0; i < RF_SLOTS; i++)
+		if (!cuda_ok(cudaMalloc(&g.raw[i], cap))) return false;
+	g.raw_cap = cap;
+	return true;
+}
+
+void note_upload()
+{
+	auto now = std::chrono::steady_clock::now();
+	if (g.have_last_upload) {
+		float dt = std::chrono::duration<float>(now - g.last_upload).count();
+		g.rf_delta_index = (g.rf_delta_index + 1) % 32;
+		g.stats.rf_time_deltas[g.rf_delta_index] = dt;
+	}
+	g.last_upload = now;
+	g.have_last_upload = true;
+}
+
+uint32_t push_data_base(const void *data, uint64_t size, int32_t timeout_ms)
+{
+	if (size > BEAMFORMER_MAX_RF_DATA_SIZE) return fail(BF_LIB_ERR_KIND_BUFFER_OVERFLOW);
+	if (!data && size) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	if (!ensure_cuda()) return 0;
+	int slot = (int)(g.insert_index % RF_SLOTS);
+	/* the slot may still be read by an in-flight compute (the reference's upload
+	 * thread waits on the slot's compute fence, beamformer.c:1243-1256) */
+	if (g.slot_used[slot] && !wait_event(g.compute_done[slot], timeout_ms)) return fail(BF_LIB_ERR_KIND_SYNC_VARIABLE);
+	if (!ensure_raw_capacity(size)) return 0;
+	if (size && !cuda_ok(cudaMemcpyAsync(g.raw[slot], data, size, cudaMemcpyHostToDevice, g.upload_stream))) return 0;
+	if (!cuda_ok(cudaEventRecord(g.upload_done[slot], g.upload_stream))) return 0;
+	/* the caller may reuse its buffer as soon as this returns */
+	if (!cuda_ok(cudaEventSynchronize(g.upload_done[slot]))) return 0;
+	g.raw_size[slot] = size;
+	g.latest_slot = slot;
+	g.insert_index++;
+	g.use_ext = false;
+	note_upload();
+	return 1;
+}
+
+void collect_timings(bool block)
+{
+	for (int n = 0; n < TIMING_SLOTS; n++) {
+		PendingTiming &t = g.timing[(g.timing_next + n) % TIMING_SLOTS];
+		if (!t.active) continue;
+		if (!block && cudaEventQuery(t.ev[t.count]) != cudaSuccess) { cudaGetLastError(); continue; }
+		if (block) cudaEventSynchronize(t.ev[t.count]);
+		float *row = g.stats.times[g.stats_index % 32];
+		std::memset(row, 0, sizeof(g.stats.times[0]));
+		for (int i = 0; i < t.count; i++) {
+			float ms = 0;
+			if (cudaEventElapsedTime(&ms, t.ev[i], t.ev[i + 1]) == cudaSuccess && t.shaders[i] >= 0 &&
+			    t.shaders[i] < BeamformerShaderKind_Count)
+				row[t.shaders[i]] += ms * 1e-3f;
+			cudaGetLastError();
+		}
+		g.stats_index++;
+		t.active = false;
+	}
+}
+
+bool run_stage(int i, const void *src, uint64_t src_bytes, DeviceFrame &frame, bool &did_sum, int &sum_target)
+{
+	const Plan &pl = g.plan;
+	const int kind = pl.shaders[i];
+	const int out_idx = g.last_chan < 0 ? 0 : 1 - g.last_chan;
+	const int in_idx = g.last_chan < 0 ? 0 : g.last_chan;
+	const BeamformerParameters &bp = g.params;
+	cudaError_t err = cudaSuccess;
+
+	switch (kind) {
+	case BeamformerShaderKind_CudaDecode:
+	case BeamformerShaderKind_Decode:
+	case BeamformerShaderKind_DecodeInt16Complex:
+	case BeamformerShaderKind_DecodeFloat:
+	case BeamformerShaderKind_DecodeFloatComplex:
+	case BeamformerShaderKind_DecodeInt16ToFloat: {
+		DecodeParams p{};
+		const bool first = i == 0;
+		p.first_stage = first;
+		if (first) {
+			p.in = src;
+			switch (g.data_kind) {
+			case BeamformerDataKind_Int16Complex:   p.input = DEC_IN_I16C; p.in_elems = src_bytes / 4; break;
+			case BeamformerDataKind_Float32:        p.input = DEC_IN_F32;  p.in_elems = src_bytes / 4; break;
+			case BeamformerDataKind_Float32Complex: p.input = DEC_IN_F32C; p.in_elems = src_bytes / 8; break;
+			default:                                p.input = DEC_IN_I16;  p.in_elems = src_bytes / 2; break;
+			}
+			p.channel_map = g.d_chmap;
+		} else {
+			p.in = g.chan[in_idx];
+			p.input = kind == BeamformerShaderKind_DecodeInt16Complex ? DEC_IN_I16C : DEC_IN_F32C;
+			p.in_elems = g.chan_bytes / (p.input == DEC_IN_I16C ? 4 : 8);
+			p.channel_map = nullptr;
+		}
+		p.out = (float *)g.chan[out_idx];
+		p.out_vec2 = g.chan_bytes / 8;
+		p.hadamard = g.hadamard;
+		p.st = pl.decode_st;
+		p.output = kind == BeamformerShaderKind_DecodeInt16ToFloat ? DEC_OUT_REAL_PAIRS : DEC_OUT_COMPLEX;
+		/* samples the reference's dispatch writes: pass-2 guard (time sample < output
+		 * transmit stride) and grid width; int16 data decoded first packs two samples
+		 * per invocation */
+		const uint32_t ots = pl.decode_st.out_transmit, cov = pl.decode_invocations_x;
+		const bool pairs = first && g.data_kind == BeamformerDataKind_Int16;
+		if (p.output == DEC_OUT_REAL_PAIRS)
+			p.samples = 2 * std::min(ots, cov);
+		else if (pairs)
+			p.samples = 2 * std::min((ots + 1) / 2, cov);
+		else
+			p.samples = std::min(ots, cov);
+		/* pass-1 gather guard: time sample < input transmit stride */
+		p.in_limit = first ? (pairs ? (pl.decode_st.in_transmit + 1) / 2 * 2 : pl.decode_st.in_transmit) : 0xFFFFFFFFu;
+		p.channels = bp.dec_data_dim[1];
+		p.transmits = pl.transmit_count;
+		p.sylvester = (uint32_t)g.hadamard_sylvester;
+		p.base = (uint32_t)g.hadamard_base;
+		p.hadamard_mode = pl.decode_mode == DECODE_MODE_HADAMARD;
+		err = launch_decode(p, g.stream);
+		g.last_chan = out_idx;
+	} break;
+	case BeamformerShaderKind_Demodulate:
+	case BeamformerShaderKind_DemodulateFloat:
+	case BeamformerShaderKind_Filter: {
+		FilterParams p{};
+		const bool is_filter = kind == BeamformerShaderKind_Filter;
+		const bool map = !is_filter && pl.demod_map;
+		p.kind = is_filter ? FILT_COMPLEX : kind == BeamformerShaderKind_Demodulate ? FILT_DEMOD_I16 : FILT_DEMOD_F32;
+		if (map) {
+			p.in = src;
+			p.in_elems = src_bytes / (p.kind == FILT_DEMOD_I16 ? 4 : 8);
+		} else {
+			p.in = g.chan[in_idx];
+			p.in_elems = g.chan_bytes / 8;
+		}
+		p.out = g.chan[out_idx];
+		p.out_elems = g.chan_bytes / (p.kind == FILT_DEMOD_I16 ? 4 : 8);
+		p.st = is_filter ? pl.filter_st : pl.demod_st;
+		p.decimation = is_filter ? 1 : pl.demod_decimation;
+		p.map_channels = map;
+		p.channel_map = g.d_chmap;
+		p.out_samples = map ? p.st.out_channel / p.st.out_sample : p.st.out_transmit;
+		p.in_samples = p.out_samples * p.decimation;
+		p.channels = pl.das.dec_data_dim[1];
+		p.transmits = pl.das.dec_data_dim[2];
+		p.taps = g.stage_tables[i].taps;
+		p.phasor = g.stage_tables[i].phasor;
+		p.taps_len = (uint32_t)g.taps[pl.slots[i] % BEAMFORMER_FILTER_SLOTS].size();
+		err = launch_filter(p, g.stream);
+		g.last_chan = out_idx;
+	} break;
+	case BeamformerShaderKind_DAS:
+	case BeamformerShaderKind_DASFast: {
+		const BeamformerParameters &d = pl.das;
+		DasParams p{};
+		p.rf = g.chan[in_idx];
+		uint64_t readable = pl.rf_size / 8;
+		p.rf_count = (int64_t)(readable < g.chan_bytes / 8 ? readable : g.chan_bytes / 8);
+		p.frame = frame.data;
+		std::memcpy(p.dims, frame.dims, sizeof(p.dims));
+		std::memcpy(p.M, g.M, sizeof(p.M));
+		std::memcpy(p.X, d.xdc_transform, sizeof(p.X));
+		p.S = (int32_t)d.dec_data_dim[0];
+		p.C = (int32_t)d.dec_data_dim[1];
+		p.T = (int32_t)d.dec_data_dim[2];
+		p.das_id = (int32_t)d.das_shader_id;
+		switch (d.das_shader_id) {
+		case DASShaderKind_FORCES: case DASShaderKind_UFORCES:       p.family = DAS_FORCES; break;
+		case DASShaderKind_HERCULES: case DASShaderKind_UHERCULES:   p.family = DAS_HERCULES; break;
+		case DASShaderKind_RCA_VLS: case DASShaderKind_RCA_TPW:
+		case DASShaderKind_FLASH:                                     p.family = DAS_RCA; break;
+		default:                                                      p.family = DAS_NONE; break;
+		}
+		p.sparse_mode = d.das_shader_id == DASShaderKind_UFORCES || d.das_shader_id == DASShaderKind_UHERCULES;
+		p.fast = kind == BeamformerShaderKind_DASFast;
+		p.coherency = d.coherency_weighting != 0;
+		p.interp = g.interpolation_override >= 0 ? g.interpolation_override : (d.interpolate ? INTERP_CUBIC : INTERP_NEAREST);
+		p.tx_rows = !((d.transmit_mode & 2) != 0);
+		p.rx_cols = (d.transmit_mode & 1) != 0;
+		p.rx_rows = !p.rx_cols;
+		p.loop_end = (d.das_shader_id == DASShaderKind_RCA_VLS || d.das_shader_id == DASShaderKind_RCA_TPW) ? p.T : p.C;
+		p.fs = d.sampling_frequency;
+		p.fc = d.center_frequency;
+		p.c = d.speed_of_sound;
+		p.toff = d.time_offset;
+		const float r360 = 360.0f * DEG2RAD_F;
+		p.r360_fc = r360 * d.center_frequency;
+		p.apod_scale = d.f_number * (180.0f * DEG2RAD_F);
+		p.apod_hi = 0.25f * r360;
+		p.inv_sqrt_T = 1.0f / sqrtf((float)p.T);
+		p.px = d.xdc_element_pitch[0];
+		p.py = d.xdc_element_pitch[1];
+		p.cy_forces = p.py * (float)(p.C / 2);
+		p.focal = g.d_focal;
+		p.sparse = g.d_sparse;
+		p.rc = 1.0f / p.c;
+		p.rfs = 1.0f / p.fs;
+		/* distances from 61 um to 8 m, sample indices from 1/256 to 65536 */
+		if (!division_range(p.c, 0x1p-14f, 8.0f, p.c_lo, p.c_hi)) return false;
+		if (!division_range(p.fs, 0x1p-8f, 65536.0f, p.fs_lo, p.fs_hi)) return false;
+		/* small volumes: split the outer loop over block groups so the grid fills the GPU */
+		p.groups = 1;
+		p.per_group = p.loop_end;
+		const int64_t nv = (int64_t)frame.dims[0] * frame.dims[1] * frame.dims[2];
+		const int64_t vblocks = (int64_t)((frame.dims[0] + 7) / 8) * frame.dims[1] * ((frame.dims[2] + 15) / 16);
+		if (p.fast && p.loop_end > 1 && vblocks < 2048) {
+			int64_t want = (2048 + vblocks - 1) / vblocks;
+			if (want > p.loop_end) want = p.loop_end;
+			p.per_group = (int32_t)((p.loop_end + want - 1) / want);
+			p.groups = (p.loop_end + p.per_group - 1) / p.per_group;
+		}
+		if (p.groups > 1) {
+			const uint64_t need = (uint64_t)p.groups * (uint64_t)nv * sizeof(float2);
+			if (need > g.das_partial_bytes) {
+				cudaStreamSynchronize(g.stream);
+				cudaFree(g.das_partial);
+				g.das_partial = nullptr;
+				g.das_partial_bytes = 0;
+				if (!cuda_ok(cudaMalloc(&g.das_partial, need))) return false;
+				g.das_partial_bytes = need;
+			}
+			p.partial = g.das_partial;
+		}
+		err = launch_das(p, g.stream);
+		frame.written = true;
+	} break;
+	case BeamformerShaderKind_Sum: {
+		int32_t n = pl.das.output_points[3];
+		if (n < 0) n = 0;
+		if (n > MAX_BEAMFORMED_SAVED_FRAMES) n = MAX_BEAMFORMED_SAVED_FRAMES;
+		const uint32_t base = g.frame_counter % MAX_BEAMFORMED_SAVED_FRAMES;
+		const float2 *ins[MAX_BEAMFORMED_SAVED_FRAMES] = {};
+		for (int32_t k = 0; k < n; k++) {
+			uint32_t idx = (base + MAX_BEAMFORMED_SAVED_FRAMES + 1 - (uint32_t)n + (uint32_t)k) % MAX_BEAMFORMED_SAVED_FRAMES;
+			DeviceFrame &f = g.frames[idx];
+			bool same = f.data && f.written && f.dims[0] == frame.dims[0] && f.dims[1] == frame.dims[1] &&
+			            f.dims[2] == frame.dims[2];
+			ins[k] = same ? f.data : nullptr;
+		}
+		const int ai = (int)(g.averaged_counter % 2);
+		DeviceFrame &af = g.averaged[ai];
+		if (!ensure_frame(af, frame.dims)) return false;
+		err = launch_sum(af.data, ins, n, 1.0f / (float)n, frame.dims, g.stream);
+		af.written = true;
+		did_sum = true;
+		sum_target = ai;
+	} break;
+	case BeamformerShaderKind_MinMax:
+		if (frame.mips > 1) err = launch_min_max(frame.data, frame.dims, frame.mips, frame.levels, g.stream);
+		break;
+	default:
+		return fail(BF_LIB_ERR_KIND_UNSUPPORTED), false;
+	}
+	return cuda_ok(err);
+}
+
+uint32_t compute_base()
+{
+	if (!ensure_cuda()) return 0;
+	if (!g.use_ext && g.latest_slot < 0) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	if (g.shader_count == 0) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	if (!prepare()) return 0;
+
+	const void *src;
+	uint64_t src_bytes;
+	int slot = -1;
+	if (g.use_ext) {
+		src = g.ext_rf;
+		src_bytes = g.ext_size;
+	} else {
+		slot = g.latest_slot;
+		src = g.raw[slot];
+		src_bytes = g.raw_size[slot];
+		if (!cuda_ok(cudaStreamWaitEvent(g.stream, g.upload_done[slot], 0))) return 0;
+	}
+
+	int32_t dims[3];
+	for (int i = 0; i < 3; i++) dims[i] = g.params.output_points[i] > 1 ? g.params.output_points[i] : 1;
+	const int fi = (int)(g.frame_counter % MAX_BEAMFORMED_SAVED_FRAMES);
+	DeviceFrame &frame = g.frames[fi];
+	if (!ensure_frame(frame, dims)) return 0;
+
+	collect_timings(false);
+	PendingTiming &tm = g.timing[g.timing_next % TIMING_SLOTS];
+	if (tm.active) collect_timings(true);
+	g.timing_next++;
+	tm.count = g.plan.count;
+	cudaEventRecord(tm.ev[0], g.stream);
+
+	g.last_chan = -1;
+	bool did_sum = false;
+	int sum_target = -1;
+	for (int i = 0; i < g.plan.count; i++) {
+		if (!run_stage(i, src, src_bytes, frame, did_sum, sum_target)) return 0;
+		tm.shaders[i] = g.plan.shaders[i];
+		cudaEventRecord(tm.ev[i + 1], g.stream);
+	}
+	tm.active = true;
+
+	cudaEvent_t done = g.use_ext ? g.ext_done : g.compute_done[slot];
+	if (!cuda_ok(cudaEventRecord(done, g.stream))) return 0;
+	if (slot >= 0) g.slot_used[slot] = true;
+	g.last_done = done;
+
+	g.latest_das_index = fi;
+	if (did_sum) {
+		g.latest_kind = 1;
+		g.latest_index = sum_target;
+		g.averaged_counter++;
+	} else {
+		g.latest_kind = 0;
+		g.latest_index = fi;
+	}
+	g.frame_counter++;
+	return 1;
+}
+
+uint32_t compute_indirect(uint32_t tag)
+{
+	if (tag >= BeamformerViewPlaneTag_Count) return fail(BF_LIB_ERR_KIND_INVALID_IMAGE_PLANE);
+	return compute_base();
+}
+
+DeviceFrame *latest_frame(uint32_t which)
+{
+	if (which == 0) return g.latest_das_index >= 0 ? &g.frames[g.latest_das_index] : nullptr;
+	if (which == 1) return (g.averaged_counter > 0) ? &g.averaged[(g.averaged_counter - 1) % 2] : nullptr;
+	if (g.latest_kind == 1) return &g.averaged[g.latest_index];
+	if (g.latest_kind == 0) return &g.frames[g.latest_index];
+	return nullptr;
+}
+
+const char *error_text(int32_t kind)
+{
+	/* kinds 0..13 as the reference words them (ogl_beamformer_lib_base.h:10-24) */
+	static const char *table[] = {
+		"None",
+		"host-library version mismatch",
+		"library in invalid state",
+		"compute stage overflow: maximum stages: 16",
+		"invalid compute shader stage",
+		"starting shader not Decode or Demodulate",
+		"data kind for demodulation not Int16 or Float",
+		"invalid image plane",
+		"passed buffer size exceeds available space",
+		"work queue full",
+		"not enough space for data export",
+		"failed to open shared memory region",
+		"failed to acquire lock within timeout period",
+		"invalid timeout value",
+		"no usable CUDA device",
+		"CUDA runtime error",
+		"unsupported pipeline configuration",
+		"invalid error kind",
+	};
+	const int32_t n = (int32_t)(sizeof(table) / sizeof(table[0]));
+	if (kind < 0 || kind >= n - 1) return table[n - 1];
+	return table[kind];
+}
+
+} /* namespace */
+
+extern "C" {
+
+LIB_FN uint32_t beamformer_get_api_version(void) { return BEAMFORMER_SHARED_MEMORY_VERSION; }
+
+LIB_FN BeamformerLibErrorKind beamformer_get_last_error(void) { return g.last_error; }
+
+LIB_FN const char *beamformer_error_string(BeamformerLibErrorKind kind) { return error_text((int32_t)kind); }
+
+LIB_FN const char *beamformer_get_last_error_string(void) { return error_text((int32_t)g.last_error); }
+
+LIB_FN uint32_t beamformer_set_global_timeout(int32_t timeout_ms)
+{
+	if (timeout_ms < -1) return fail(BF_LIB_ERR_KIND_INVALID_TIMEOUT);
+	g.timeout_ms = timeout_ms;
+	return 1;
+}
+
+LIB_FN uint32_t beamformer_push_pipeline(int32_t *shaders, int32_t shader_count, BeamformerDataKind data_kind)
+{
+	/* validate_pipeline (ogl_beamformer_lib.c:166-190) */
+	if (shader_count > MAX_COMPUTE_SHADER_STAGES) return fail(BF_LIB_ERR_KIND_COMPUTE_STAGE_OVERFLOW);
+	if (shader_count < 1 || !shaders) return fail(BF_LIB_ERR_KIND_INVALID_START_SHADER);
+	for (int32_t i = 0; i < shader_count; i++)
+		if (shaders[i] < 0 || shaders[i] > BeamformerShaderKind_ComputeCount)
+			return fail(BF_LIB_ERR_KIND_INVALID_COMPUTE_STAGE);
+	if (shaders[0] != BeamformerShaderKind_Demodulate && shaders[0] != BeamformerShaderKind_Decode)
+		return fail(BF_LIB_ERR_KIND_INVALID_START_SHADER);
+	if (shaders[0] == BeamformerShaderKind_Demodulate &&
+	    !(data_kind == BeamformerDataKind_Int16 || data_kind == BeamformerDataKind_Float32))
+		return fail(BF_LIB_ERR_KIND_INVALID_DEMOD_DATA_KIND);
+	g.shader_count = shader_count;
+	g.data_kind = (int32_t)data_kind;
+	for (int32_t i = 0; i < shader_count; i++) g.shaders[i] = shaders[i];
+	g.dirty = true;
+	return 1;
+}
+
+LIB_FN uint32_t beamformer_set_pipeline_stage_parameters(int32_t stage_index, int32_t parameter)
+{
+	if (g.shader_count == 0) return 0;
+	int32_t s = stage_index % MAX_COMPUTE_SHADER_STAGES;
+	if (s < 0) s += MAX_COMPUTE_SHADER_STAGES;
+	g.slots[s] = (uint8_t)parameter;
+	g.dirty = true;
+	return 1;
+}
+
+static uint32_t create_filter(int32_t kind, float p0, float p1, float fs, int16_t length, uint8_t slot)
+{
+	if (length < 1 || !(fs > 0)) return fail(BF_LIB_ERR_KIND_UNSUPPORTED);
+	const int s = slot % BEAMFORMER_FILTER_SLOTS;
+	FilterSpec &f = g.filters[s];
+	f.kind = kind; f.length = length; f.sampling_frequency = fs; f.param0 = p0; f.param1 = p1;
+	g.taps[s].assign((size_t)length, 0.0f);
+	if (kind == BeamformerFilterKind_Kaiser) kaiser_low_pass(p1, fs, p0, length, g.taps[s].data());
+	else                                      matched_filter(p0, p1, fs, length, g.taps[s].data());
+	g.dirty = true;
+	return 1;
+}
+
+LIB_FN uint32_t beamformer_create_kaiser_low_pass_filter(float beta, float cutoff_frequency, float sampling_frequency,
+                                                         int16_t length, uint8_t slot)
+{
+	return create_filter(BeamformerFilterKind_Kaiser, beta, cutoff_frequency, sampling_frequency, length, slot);
+}
+
+LIB_FN uint32_t beamformer_create_matched_filter(float xdc_center_frequency, float transmit_frequency,
+                                                 float sampling_frequency, int16_t length, uint8_t slot)
+{
+	return create_filter(BeamformerFilterKind_Matched, xdc_center_frequency, transmit_frequency, sampling_frequency,
+	                     length, slot);
+}
+
+LIB_FN uint32_t beamformer_push_channel_mapping(int16_t *mapping, uint32_t count)
+{
+	if (count > 256) return fail(BF_LIB_ERR_KIND_BUFFER_OVERFLOW);
+	if (count && !mapping) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	std::memcpy(g.channel_mapping, mapping, count * sizeof(int16_t));
+	g.dirty = true;
+	return 1;
+}
+
+LIB_FN uint32_t beamformer_push_sparse_elements(int16_t *elements, uint32_t count)
+{
+	if (count > 256) return fail(BF_LIB_ERR_KIND_BUFFER_OVERFLOW);
+	if (count && !elements) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	std::memcpy(g.sparse_elements, elements, count * sizeof(int16_t));
+	g.dirty = true;
+	return 1;
+}
+
+LIB_FN uint32_t beamformer_push_focal_vectors(float *vectors, uint32_t count)
+{
+	if (count > 256) return fail(BF_LIB_ERR_KIND_BUFFER_OVERFLOW);
+	if (count && !vectors) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	std::memcpy(g.focal_vectors, vectors, count * 2 * sizeof(float));
+	g.dirty = true;
+	return 1;
+}
+
+LIB_FN uint32_t beamformer_push_parameters(BeamformerParameters *bp)
+{
+	if (!bp) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	g.params = *bp;
+	g.dirty = true;
+	return 1;
+}
+
+LIB_FN uint32_t beamformer_push_parameters_ui(BeamformerUIParameters *ui)
+{
+	if (!ui) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	std::memcpy((char *)&g.params + offsetof(BeamformerParameters, output_min_coordinate), ui, sizeof(*ui));
+	g.dirty = true;
+	return 1;
+}
+
+LIB_FN uint32_t beamformer_push_parameters_head(BeamformerParametersHead *head)
+{
+	if (!head) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	std::memcpy(&g.params, head, sizeof(*head));
+	g.dirty = true;
+	return 1;
+}
+
+LIB_FN uint32_t beamformer_push_data(void *data, uint32_t size)
+{
+	return push_data_base(data, size, g.timeout_ms);
+}
+
+LIB_FN uint32_t beamformer_push_data_with_compute(void *data, uint32_t size, uint32_t image_plane_tag)
+{
+	uint32_t r = push_data_base(data, size, g.timeout_ms);
+	if (r) r = compute_indirect(image_plane_tag);
+	return r;
+}
+
+LIB_FN uint32_t beamformer_start_compute(void) { return compute_indirect(0); }
+
+LIB_FN uint32_t beamformer_wait_for_compute_dispatch(int32_t timeout_ms)
+{
+	/* compute is dispatched onto the stream by the call that requests it */
+	(void)timeout_ms;
+	return 1;
+}
+
+LIB_FN uint32_t beamform_data_synchronized(void *data, uint32_t data_size, int32_t output_points[3], float *out_data,
+                                           int32_t timeout_ms)
+{
+	if (!output_points) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	for (int i = 0; i < 3; i++) {
+		output_points[i] = output_points[i] > 1 ? output_points[i] : 1;
+		if (g.params.output_points[i] != output_points[i]) {
+			g.params.output_points[i] = output_points[i];
+			g.dirty = true;
+		}
+	}
+	uint64_t out_size = (uint64_t)(uint32_t)output_points[0] * (uint32_t)output_points[1] * (uint32_t)output_points[2] *
+	                    sizeof(float) * 2;
+	if (out_size > SCRATCH_SIZE) return fail(BF_LIB_ERR_KIND_EXPORT_SPACE_OVERFLOW);
+	if (!beamformer_push_data_with_compute(data, data_size, 0)) return 0;
+	if (!wait_event(g.last_done, timeout_ms)) return fail(BF_LIB_ERR_KIND_SYNC_VARIABLE);
+	DeviceFrame *f = latest_frame(2);
+	if (!f || !f->data) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	uint64_t have = (uint64_t)f->dims[0] * f->dims[1] * f->dims[2] * sizeof(float2);
+	if (have > out_size) return fail(BF_LIB_ERR_KIND_EXPORT_SPACE_OVERFLOW);
+	if (!out_data) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	if (!cuda_ok(cudaMemcpyAsync(out_data, f->data, have, cudaMemcpyDeviceToHost, g.stream))) return 0;
+	if (!cuda_ok(cudaStreamSynchronize(g.stream))) return 0;
+	return 1;
+}
+
+LIB_FN uint32_t beamformer_compute_timings(BeamformerComputeStatsTable *output, int32_t timeout_ms)
+{
+	if (!output) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	if (g.ready) {
+		if (g.last_done && !wait_event(g.last_done, timeout_ms)) return fail(BF_LIB_ERR_KIND_SYNC_VARIABLE);
+		collect_timings(false);
+	}
+	*output = g.stats;
+	return 1;
+}
+
+LIB_FN int32_t beamformer_live_parameters_get_dirty_flag(void)
+{
+	if (!g.live_dirty) return -1;
+	int32_t flag = __builtin_ctz(g.live_dirty);
+	g.live_dirty &= ~(1u << flag);
+	return flag;
+}
+
+LIB_FN uint32_t beamformer_set_live_parameters(BeamformerLiveImagingParameters *lp)
+{
+	if (!lp) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	g.live = *lp;
+	return 1;
+}
+
+LIB_FN BeamformerLiveImagingParameters *beamformer_get_live_parameters(void) { return &g.live; }
+
+/* ------------------------------- extensions ------------------------------ */
+
+LIB_FN uint32_t beamformer_gb300_push_data_device(const void *device_data, uint64_t size)
+{
+	if (size > BEAMFORMER_MAX_RF_DATA_SIZE) return fail(BF_LIB_ERR_KIND_BUFFER_OVERFLOW);
+	if (!device_data && size) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	if (!ensure_cuda()) return 0;
+	g.ext_rf = device_data;
+	g.ext_size = size;
+	g.use_ext = true;
+	note_upload();
+	return 1;
+}
+
+LIB_FN uint32_t beamformer_gb300_set_stream(void *cuda_stream)
+{
+	if (!ensure_cuda()) return 0;
+	g.stream = cuda_stream ? (cudaStream_t)cuda_stream : g.own_stream;
+	return 1;
+}
+
+LIB_FN void *beamformer_gb300_get_stream(void)
+{
+	if (!ensure_cuda()) return nullptr;
+	return (void *)g.stream;
+}
+
+LIB_FN uint32_t beamformer_gb300_synchronize(int32_t timeout_ms)
+{
+	if (!g.ready) return 1;
+	if (!wait_event(g.last_done, timeout_ms)) return fail(BF_LIB_ERR_KIND_SYNC_VARIABLE);
+	return cuda_ok(cudaStreamSynchronize(g.stream)) ? 1 : 0;
+}
+
+LIB_FN uint32_t beamformer_gb300_export_frame(uint32_t which, uint32_t mip_level, float *out, uint64_t out_size,
+                                              int32_t dims_out[3])
+{
+	if (!g.ready) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	DeviceFrame *f = latest_frame(which);
+	if (!f || !f->data) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	if ((int32_t)mip_level >= f->mips) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	const float2 *src = f->data;
+	int32_t d[3] = {f->dims[0], f->dims[1], f->dims[2]};
+	if (mip_level > 0) {
+		src = f->levels;
+		for (uint32_t l = 1; l <= mip_level; l++) {
+			int32_t x = f->dims[0] >> l, y = f->dims[1] >> l, z = f->dims[2] >> l;
+			x = x ? x : 1; y = y ? y : 1; z = z ? z : 1;
+			if (l < mip_level) src += (uint64_t)x * y * z;
+			d[0] = x; d[1] = y; d[2] = z;
+		}
+	}
+	if (dims_out) std::memcpy(dims_out, d, sizeof(d));
+	uint64_t bytes = (uint64_t)d[0] * d[1] * d[2] * sizeof(float2);
+	if (!out) return 1;
+	if (bytes > out_size) return fail(BF_LIB_ERR_KIND_EXPORT_SPACE_OVERFLOW);
+	if (!cuda_ok(cudaStreamSynchronize(g.stream))) return 0;
+	return cuda_ok(cudaMemcpy(out, src, bytes, cudaMemcpyDeviceToHost)) ? 1 : 0;
+}
+
+LIB_FN uint32_t beamformer_gb300_export_channel_data(void *out, uint64_t out_size, uint64_t *size_out)
+{
+	if (!g.ready || g.last_chan < 0) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	if (size_out) *size_out = g.chan_bytes;
+	if (!out) return 1;
+	if (g.chan_bytes > out_size) return fail(BF_LIB_ERR_KIND_EXPORT_SPACE_OVERFLOW);
+	if (!cuda_ok(cudaStreamSynchronize(g.stream))) return 0;
+	return cuda_ok(cudaMemcpy(out, g.chan[g.last_chan], g.chan_bytes, cudaMemcpyDeviceToHost)) ? 1 : 0;
+}
+
+LIB_FN uint32_t beamformer_gb300_get_filter(uint8_t slot, float *taps, int32_t capacity, int32_t *length_out)
+{
+	const int s = slot % BEAMFORMER_FILTER_SLOTS;
+	const int32_t n = (int32_t)g.taps[s].size();
+	if (length_out) *length_out = n;
+	if (!taps) return 1;
+	if (capacity < n) return fail(BF_LIB_ERR_KIND_BUFFER_OVERFLOW);
+	std::memcpy(taps, g.taps[s].data(), (size_t)n * sizeof(float));
+	return 1;
+}
+
+LIB_FN uint32_t beamformer_gb300_set_interpolation(int32_t mode)
+{
+	if (mode < -1 || mode > 2) return fail(BF_LIB_ERR_KIND_UNSUPPORTED);
+	g.interpolation_override = mode;
+	return 1;
+}
+
+LIB_FN uint64_t beamformer_gb300_kernel_launch_count(void) { return g_kernel_launches; }
+
+LIB_FN void beamformer_gb300_shutdown(void)
+{
+	if (!g.ready) return;
+	cudaDeviceSynchronize();
+	for (auto &f : g.frames) free_frame(f);
+	for (auto &f : g.averaged) free_frame(f);
+	for (int i = 0; i < RF_SLOTS; i++) {
+		cudaFree(g.raw[i]);
+		cudaEventDestroy(g.upload_done[i]);
+		cudaEventDestroy(g.compute_done[i]);
+	}
+	cudaEventDestroy(g.ext_done);
+	for (auto &t : g.timing)
+		for (auto &e : t.ev) cudaEventDestroy(e);
+	cudaFree(g.chan[0]); cudaFree(g.chan[1]);
+	cudaFree(g.hadamard);
+	cudaFree(g.das_partial);
+	cudaFree(g.d_mismatch);
+	cudaFree(g.d_chmap); cudaFree(g.d_sparse); cudaFree(g.d_focal);
+	for (auto &st : g.stage_tables) { cudaFree(st.taps); cudaFree(st.phasor); }
+	cudaStreamDestroy(g.own_stream);
+	cudaStreamDestroy(g.upload_stream);
+	/* keep what the caller pushed; drop every device object */
+	Context fresh;
+	fresh.params = g.params;
+	std::memcpy(fresh.shaders, g.shaders, sizeof(g.shaders));
+	std::memcpy(fresh.slots, g.slots, sizeof(g.slots));
+	fresh.shader_count = g.shader_count;
+	fresh.data_kind = g.data_kind;
+	std::memcpy(fresh.channel_mapping, g.channel_mapping, sizeof(g.channel_mapping));
+	std::memcpy(fresh.sparse_elements, g.sparse_elements, sizeof(g.sparse_elements));
+	std::memcpy(fresh.focal_vectors, g.focal_vectors, sizeof(g.focal_vectors));
+	for (int i = 0; i < BEAMFORMER_FILTER_SLOTS; i++) { fresh.filters[i] = g.filters[i]; fresh.taps[i] = g.taps[i]; }
+	fresh.timeout_ms = g.timeout_ms;
+	fresh.interpolation_override = g.interpolation_override;
+	g = fresh;
+}
+
+} /* extern "C" */

@@ -129,7 +129,8 @@ int32_t bfo_hadamard_transpose(int32_t dim, int32_t *out)
 	}
 	if (!base || !is_pow2(order)) return 0;
 
-	int32_t *m = (base == dim) ? out : (int32_t *)malloc(sizeof(int32_t) * (size_t)order * (size_t)order);
+	const int kron = order != dim;   /* a 12 or 20 Paley factor is present */
+	int32_t *m = !kron ? out : (int32_t *)malloc(sizeof(int32_t) * (size_t)order * (size_t)order);
 	m[0] = 1;
 	for (int32_t k = 1; k < order; k *= 2) {
 		for (int32_t i = 0; i < k; i++) {
@@ -141,7 +142,7 @@ int32_t bfo_hadamard_transpose(int32_t dim, int32_t *out)
 			}
 		}
 	}
-	if (base != dim) {
+	if (kron) {
 		int32_t small[400];
 		paley_bordered(base - 1, small);
 		for (int32_t bi = 0; bi < order; bi++)

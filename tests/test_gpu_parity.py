@@ -1,0 +1,170 @@
+"""GPU parity: every stage of the CUDA pipeline against the CPU oracle, through the
+C ABI (decode bit-exact; float stages NRMSE <= -80 dB and max-abs <= 1e-4 of peak).
+"""
+import numpy as np
+import pytest
+
+from ogl_beamforming_cuda_gb300 import abi, synth
+from bf_cases import small_params, small_raw, run_both, check_volume
+
+pytestmark = pytest.mark.gpu
+SH = abi.SHADER
+DK = abi.DATA_KIND
+
+def perm_map(n, seed=5):
+    return np.concatenate([np.random.default_rng(seed).permutation(n), np.arange(n, 256)]).astype(np.int16)
+
+
+TEST_MAP = perm_map(16)
+
+
+@pytest.mark.parametrize("T", [2, 4, 8, 16, 32, 64, 128])
+@pytest.mark.parametrize("to_float", [False, True])
+def test_decode_sylvester_bit_exact(T, to_float):
+    bp = small_params(S=256, C=16, T=T)
+    raw = np.random.default_rng(T).integers(-32768, 32767, size=(16, T, 256), dtype=np.int16)
+    pipe = [SH["Decode"], SH["Demodulate"]] if to_float else [SH["Decode"]]
+    bf, ref = run_both(bp, pipe, raw, chmap=TEST_MAP)
+    got = bf.channel_data()
+    exp = ref["channel_data"]
+    if to_float:
+        check_volume(got, exp, "decode->demod")
+    else:
+        assert np.array_equal(got.view(np.uint32), exp.view(np.uint32))
+
+
+@pytest.mark.parametrize("T", [12, 20, 24, 40, 256])
+def test_decode_kronecker_and_large_orders_bit_exact(T):
+    bp = small_params(S=128, C=8, T=T)
+    raw = np.random.default_rng(T).integers(-32768, 32767, size=(8, T, 128), dtype=np.int16)
+    bf, ref = run_both(bp, [SH["Decode"]], raw)
+    assert np.array_equal(bf.channel_data().view(np.uint32), ref["channel_data"].view(np.uint32))
+
+
+@pytest.mark.parametrize("kind,shape,dtype", [
+    ("Int16Complex", (8, 16, 64, 2), np.int16), ("Float32", (8, 16, 64), np.float32),
+    ("Float32Complex", (8, 16, 64, 2), np.float32)])
+def test_decode_other_data_kinds(kind, shape, dtype):
+    bp = small_params(S=64, C=8, T=16)
+    rng = np.random.default_rng(11)
+    raw = (rng.integers(-30000, 30000, size=shape).astype(dtype) if dtype == np.int16
+           else rng.standard_normal(shape).astype(dtype))
+    bf, ref = run_both(bp, [SH["Decode"]], raw, data_kind=DK[kind])
+    assert np.array_equal(bf.channel_data().view(np.uint32), ref["channel_data"].view(np.uint32))
+
+
+def test_decode_mode_none_reshapes():
+    bp = small_params(S=64, C=8, T=16)
+    bp.decode = 0
+    raw = np.random.default_rng(2).integers(-32768, 32767, size=(8, 16, 64), dtype=np.int16)
+    bf, ref = run_both(bp, [SH["Decode"]], raw, chmap=perm_map(8))
+    assert np.array_equal(bf.channel_data().view(np.uint32), ref["channel_data"].view(np.uint32))
+
+
+@pytest.mark.parametrize("D,L", [(1, 16), (2, 32), (2, 64), (4, 64), (3, 37)])
+def test_demodulate_fir(D, L):
+    bp = small_params(S=512, C=16, T=16, D=D)
+    raw = small_raw(bp)
+    bf, ref = run_both(bp, [SH["Decode"], SH["Demodulate"]], raw, kaiser=(5.65, 5e6, 25e6, L))
+    check_volume(bf.channel_data(), ref["channel_data"], f"demod D={D} L={L}")
+
+
+def test_matched_filter_stage():
+    bp = small_params(S=512, C=16, T=16, D=2)
+    raw = small_raw(bp)
+    pipe = [SH["Decode"], SH["Demodulate"], SH["Filter"]]
+    bf, ref = run_both(bp, pipe, raw, matched=(12.5e6, 12.5e6, 12.5e6 * 4, 20, 1), slots={2: 1})
+    check_volume(bf.channel_data(), ref["channel_data"], "decode->demod->matched filter")
+
+
+def test_demodulate_first_int16_snorm_then_decode():
+    bp = small_params(S=512, C=16, T=16, D=2)
+    raw = small_raw(bp)
+    bf, ref = run_both(bp, [SH["Demodulate"], SH["Decode"]], raw, chmap=perm_map(16))
+    check_volume(bf.channel_data(), ref["channel_data"], "demod(i16)->decode")
+
+
+def test_demodulate_first_float_then_decode():
+    bp = small_params(S=512, C=16, T=16, D=2)
+    raw = small_raw(bp).astype(np.float32) / 16384.0
+    bf, ref = run_both(bp, [SH["Demodulate"], SH["Decode"]], raw, data_kind=DK["Float32"])
+    check_volume(bf.channel_data(), ref["channel_data"], "demod(f32)->decode")
+
+
+DAS_CASES = [(das, interp, coh) for das in ("HERCULES", "UHERCULES", "FORCES", "UFORCES", "RCA_TPW", "RCA_VLS", "FLASH")
+             for interp in (0, 1, 2) for coh in (0, 1)]
+
+
+@pytest.mark.parametrize("das,interp,coh", DAS_CASES)
+def test_das_modes(das, interp, coh):
+    bp = small_params(S=512, C=16, T=16, points=(16, 3, 20), das=das, coherency=coh)
+    raw = small_raw(bp)
+    rng = np.random.default_rng(9)
+    focal = np.zeros(512, np.float32)
+    focal[0::2] = rng.uniform(-8, 8, 256)
+    focal[1::2] = np.where(rng.random(256) < 0.5, np.inf, rng.uniform(5e-3, 3e-2, 256))
+    focal[0], focal[1] = 0.0, np.inf
+    sparse = rng.permutation(16).astype(np.int16)
+    sparse = np.concatenate([sparse, np.arange(16, 256, dtype=np.int16)])
+    bf, ref = run_both(bp, [SH["Decode"], SH["Demodulate"], SH["DAS"]], raw, focal=focal, sparse=sparse,
+                       interpolation=interp)
+    vol, dims = bf.frame(0)
+    check_volume(vol, ref["frame"], f"DAS {das} interp={interp} coherency={coh}")
+
+
+def test_das_unknown_kind_is_zero():
+    bp = small_params(S=512, C=16, T=16, das="RACES")
+    raw = small_raw(bp)
+    bf, ref = run_both(bp, [SH["Decode"], SH["Demodulate"], SH["DAS"]], raw)
+    vol, _ = bf.frame(0)
+    assert not np.any(vol) and not np.any(ref["frame"])
+
+
+def test_das_without_demodulation_uses_no_phase():
+    bp = small_params(S=256, C=16, T=16, D=1)
+    raw = small_raw(bp)
+    bf, ref = run_both(bp, [SH["Decode"], SH["DAS"]], raw, kaiser=None)
+    check_volume(bf.frame(0)[0], ref["frame"], "decode->DAS (fc = 0)")
+
+
+def test_sum_and_min_max_bit_exact():
+    bp = small_params(S=512, C=16, T=16, points=(64, 2, 64), frames=4)
+    pipe = [SH["Decode"], SH["Demodulate"], SH["DAS"], SH["Sum"], SH["MinMax"]]
+    from ogl_beamforming_cuda_gb300.client import Beamformer
+    from oracle.bf_oracle import OraclePipeline
+    bf = Beamformer().configure(bp, pipe, kaiser=(5.65, 5e6, 25e6, 32))
+    orc = OraclePipeline()
+    orc.bp, orc.shaders = bp, pipe
+    orc.create_kaiser(5.65, 5e6, 25e6, 32, 0)
+    for seed in range(6):       # more frames than averaged: the ring wraps
+        raw = small_raw(bp, seed=seed)
+        bf.push(raw)
+        ref = orc.compute(raw)
+    bf.synchronize()
+    das, _ = bf.frame(0)
+    check_volume(das, ref["frame"], "DAS frame")
+    avg, _ = bf.frame(1)
+    check_volume(avg, ref["averaged"], "averaged frame")
+    # sum and min/max themselves are bit exact: feed the GPU frames to the oracle
+    from oracle import bf_oracle as O
+    levels = O.min_max(das, (64, 2, 64))
+    off = 0
+    mips = O.frame_mips((64, 2, 64))
+    for lvl in range(1, mips):
+        got, d = bf.frame(0, lvl)
+        n = got.size
+        assert np.array_equal(got, levels[off:off + n], equal_nan=True), f"mip {lvl}"
+        off += n
+
+
+def test_beamform_data_synchronized_matches_oracle():
+    bp = small_params(S=512, C=32, T=32, points=(32, 1, 32))
+    raw = small_raw(bp)
+    from ogl_beamforming_cuda_gb300.client import Beamformer
+    from oracle.bf_oracle import OraclePipeline
+    bf = Beamformer().configure(bp, [SH["Decode"], SH["Demodulate"], SH["DAS"]], kaiser=(5.65, 5e6, 25e6, 32))
+    vol = bf.beamform(raw)
+    orc = OraclePipeline()
+    orc.bp, orc.shaders = bp, [SH["Decode"], SH["Demodulate"], SH["DAS"]]
+    orc.create_kaiser(5.65, 5e6, 25e6, 32, 0)
+    check_volume(vol, orc.compute(raw)["frame"], "beamform_data_synchronized")
