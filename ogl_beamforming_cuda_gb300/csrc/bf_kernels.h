@@ -92,10 +92,16 @@ struct DasParams {
 	 * groups > 1 writes partial sums to `partial` (groups x voxels) */
 	int32_t        groups, per_group;
 	float2        *partial;
+	/* receive-distance square root: 1 = rsqrt + one Newton step (checked equal to
+	 * IEEE sqrt over [sqrt_lo, sqrt_hi]), 0 = IEEE sqrt */
+	int32_t        fast_sqrt;
+	int32_t        dense_rows;   /* rf holds exactly C*T*S samples (< 2^31), S >= 4: branch-free HERCULES path */
+	float          sqrt_lo, sqrt_hi;
 };
 
 /* Exhaustively compare x * rb + correction with IEEE x / b for every float x in
  * [lo, hi]; *mismatch receives the count of differing x. */
+cudaError_t launch_verify_sqrt(float lo, float hi, unsigned long long *mismatch, cudaStream_t s);
 cudaError_t launch_verify_division(float b, float rb, float lo, float hi, unsigned long long *mismatch, cudaStream_t s);
 
 /* launchers: return cudaSuccess or the launch error */

@@ -92,7 +92,8 @@ struct Context {
 	cudaEvent_t  ext_done = nullptr, last_done = nullptr;
 
 	float2      *chan[2] = {};
-	uint64_t     chan_bytes = 0;
+	uint64_t     chan_bytes = 0;         /* allocated */
+	uint64_t     chan_used = 0;          /* size the current plan uses */
 	int          last_chan = -1;
 
 	int8_t      *hadamard = nullptr;
@@ -126,6 +127,7 @@ struct Context {
 	unsigned long long *d_mismatch = nullptr;
 	struct DivCheck { float b, lo, hi; };
 	std::vector<DivCheck> div_checks;
+	int          sqrt_checked = -1;      /* -1 unknown, 0 IEEE only, 1 Newton sqrt verified */
 
 	Context()
 	{
@@ -252,6 +254,7 @@ bool prepare()
 		cudaMemsetAsync(g.chan[1], 0, need, g.stream);
 		g.chan_bytes = need;
 	}
+	g.chan_used = need;
 	/* a new plan may write only part of a channel buffer (the reference's dispatch
 	 * grid decides); start it from zeros rather than the previous plan's data */
 	cudaMemsetAsync(g.chan[0], 0, g.chan_bytes, g.stream);
@@ -360,6 +363,25 @@ bool division_range(float b, float lo, float hi, float &out_lo, float &out_hi)
 	if (bad == 0) { out_lo = lo; out_hi = hi; }
 	g.div_checks.push_back({b, out_lo, out_hi});
 	return true;
+}
+
+/* Check once whether the rsqrt + Newton square root equals IEEE sqrt on every
+ * float in [2^-40, 2^24] (squared receive distances in m^2 lie far inside). */
+bool sqrt_verified()
+{
+	if (g.sqrt_checked >= 0) return g.sqrt_checked == 1;
+	if (!g.d_mismatch && !cuda_ok(cudaMalloc(&g.d_mismatch, sizeof(unsigned long long)))) return false;
+	unsigned long long bad = 1;
+	if (cudaMemsetAsync(g.d_mismatch, 0, sizeof(bad), g.stream) == cudaSuccess &&
+	    launch_verify_sqrt(0x1p-40f, 0x1p24f, g.d_mismatch, g.stream) == cudaSuccess &&
+	    cudaMemcpyAsync(&bad, g.d_mismatch, sizeof(bad), cudaMemcpyDeviceToHost, g.stream) == cudaSuccess &&
+	    cudaStreamSynchronize(g.stream) == cudaSuccess) {
+		g.sqrt_checked = bad == 0 ? 1 : 0;
+	} else {
+		cudaGetLastError();
+		g.sqrt_checked = 0;
+	}
+	return g.sqrt_checked == 1;
 }
 
 bool ensure_raw_capacity(uint64_t size)
@@ -574,6 +596,13 @@ bool run_stage(int i, const void *src, uint64_t src_bytes, DeviceFrame &frame, b
 		/* distances from 61 um to 8 m, sample indices from 1/256 to 65536 */
 		if (!division_range(p.c, 0x1p-14f, 8.0f, p.c_lo, p.c_hi)) return false;
 		if (!division_range(p.fs, 0x1p-8f, 65536.0f, p.fs_lo, p.fs_hi)) return false;
+		p.fast_sqrt = sqrt_verified() ? 1 : 0;
+		p.sqrt_lo = 0x1p-40f;
+		p.sqrt_hi = 0x1p24f;
+		{
+			const int64_t dense = (int64_t)p.C * p.T * p.S;
+			p.dense_rows = p.rf_count >= dense && dense < (1ll << 31) && p.S >= 4;
+		}
 		/* small volumes: split the outer loop over block groups so the grid fills the GPU */
 		p.groups = 1;
 		p.per_group = p.loop_end;
@@ -998,11 +1027,11 @@ LIB_FN uint32_t beamformer_gb300_export_frame(uint32_t which, uint32_t mip_level
 LIB_FN uint32_t beamformer_gb300_export_channel_data(void *out, uint64_t out_size, uint64_t *size_out)
 {
 	if (!g.ready || g.last_chan < 0) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
-	if (size_out) *size_out = g.chan_bytes;
+	if (size_out) *size_out = g.chan_used;
 	if (!out) return 1;
-	if (g.chan_bytes > out_size) return fail(BF_LIB_ERR_KIND_EXPORT_SPACE_OVERFLOW);
+	if (g.chan_used > out_size) return fail(BF_LIB_ERR_KIND_EXPORT_SPACE_OVERFLOW);
 	if (!cuda_ok(cudaStreamSynchronize(g.stream))) return 0;
-	return cuda_ok(cudaMemcpy(out, g.chan[g.last_chan], g.chan_bytes, cudaMemcpyDeviceToHost)) ? 1 : 0;
+	return cuda_ok(cudaMemcpy(out, g.chan[g.last_chan], g.chan_used, cudaMemcpyDeviceToHost)) ? 1 : 0;
 }
 
 LIB_FN uint32_t beamformer_gb300_get_filter(uint8_t slot, float *taps, int32_t capacity, int32_t *length_out)

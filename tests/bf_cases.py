@@ -24,6 +24,18 @@ def small_raw(bp, seed=3, n_points=8, n_speckle=40):
     return synth.encode_and_quantise(synth.decoded_traces(bp, pos, amp), seed).numpy()
 
 
+def oracle_for(bf, bp, pipeline, kaiser=None, data_kind=abi.DATA_KIND["Int16"]):
+    """An oracle holding the same state the client pushed to the library."""
+    orc = OraclePipeline()
+    orc.bp = bp
+    orc.shaders = list(pipeline)
+    orc.data_kind = data_kind
+    if kaiser is not None:
+        orc.create_kaiser(kaiser[0], kaiser[1], kaiser[2], kaiser[3], 0)
+    orc.chmap, orc.focal, orc.sparse = bf.chmap, bf.focal, bf.sparse
+    return orc
+
+
 def run_both(bp, pipeline, raw, data_kind=abi.DATA_KIND["Int16"], kaiser=(5.65, 5e6, 25e6, 32), matched=None,
              chmap=None, focal=None, sparse=None, slots=None, interpolation=-1, want_frames=("frame",)):
     bf = Beamformer().configure(bp, pipeline, data_kind=data_kind, kaiser=kaiser, matched=matched,

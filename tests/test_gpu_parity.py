@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from ogl_beamforming_cuda_gb300 import abi, synth
-from bf_cases import small_params, small_raw, run_both, check_volume
+from bf_cases import small_params, small_raw, run_both, check_volume, oracle_for
 
 pytestmark = pytest.mark.gpu
 SH = abi.SHADER
@@ -133,9 +133,7 @@ def test_sum_and_min_max_bit_exact():
     from ogl_beamforming_cuda_gb300.client import Beamformer
     from oracle.bf_oracle import OraclePipeline
     bf = Beamformer().configure(bp, pipe, kaiser=(5.65, 5e6, 25e6, 32))
-    orc = OraclePipeline()
-    orc.bp, orc.shaders = bp, pipe
-    orc.create_kaiser(5.65, 5e6, 25e6, 32, 0)
+    orc = oracle_for(bf, bp, pipe, kaiser=(5.65, 5e6, 25e6, 32))
     for seed in range(6):       # more frames than averaged: the ring wraps
         raw = small_raw(bp, seed=seed)
         bf.push(raw)
@@ -164,7 +162,5 @@ def test_beamform_data_synchronized_matches_oracle():
     from oracle.bf_oracle import OraclePipeline
     bf = Beamformer().configure(bp, [SH["Decode"], SH["Demodulate"], SH["DAS"]], kaiser=(5.65, 5e6, 25e6, 32))
     vol = bf.beamform(raw)
-    orc = OraclePipeline()
-    orc.bp, orc.shaders = bp, [SH["Decode"], SH["Demodulate"], SH["DAS"]]
-    orc.create_kaiser(5.65, 5e6, 25e6, 32, 0)
+    orc = oracle_for(bf, bp, [SH["Decode"], SH["Demodulate"], SH["DAS"]], kaiser=(5.65, 5e6, 25e6, 32))
     check_volume(vol, orc.compute(raw)["frame"], "beamform_data_synchronized")
