@@ -329,6 +329,31 @@ LIB_FN uint32_t beamformer_gb300_get_filter(uint8_t slot, float *taps, int32_t c
  * Linear interpolation has no counterpart in the reference. */
 LIB_FN uint32_t beamformer_gb300_set_interpolation(int32_t mode);
 
+/* Delay-and-sum of one frame that allocates no device memory. Has no
+ * counterpart in the reference. It is meant for callers that cannot let a
+ * library allocate on the GPU while they run: for example an acquisition loop
+ * that fixes its whole memory budget at start-up, or a host application whose
+ * device memory belongs to its own allocator. Such callers cannot grant the
+ * scratch buffer the regular pipeline allocates for small volumes.
+ *   das_parameters  the parameters as the DAS stage sees them (for a
+ *                   decode -> demodulate -> DAS pipeline: dec_data_dim[0],
+ *                   sampling_frequency divided by 2 * decimation_rate,
+ *                   time_offset including the filter delays);
+ *   focal_vectors   host, 256 (angle, depth) pairs (NULL: all zero);
+ *   sparse_elements host, 256 entries (NULL: 0..255);
+ *   channel_data    device, float2 [channel][transmit][sample];
+ *   frame           device, output_points[0..2] float2 in x-fastest order;
+ *   cuda_stream     cudaStream_t as a pointer (NULL: the default stream).
+ * The partial sums of small volumes are kept in a static device array of
+ * 262144 float2 entries (2 MiB) that every GPU loading this library holds
+ * until the process exits. A call that would need more (channel groups times
+ * voxels > 262144) fails with BF_LIB_ERR_KIND_BUFFER_OVERFLOW. The first call on
+ * a device looks up the array's device address; make that first call before any
+ * stream capture. All calls share the array, so calls that overlap on the GPU race. */
+LIB_FN uint32_t beamformer_gb300_das_no_alloc(const BeamformerParameters *das_parameters, const float *focal_vectors,
+                                              const int16_t *sparse_elements, const void *channel_data,
+                                              uint64_t channel_data_bytes, float *frame, void *cuda_stream);
+
 /* Number of kernel launches this library issued since load (all streams). */
 LIB_FN uint64_t beamformer_gb300_kernel_launch_count(void);
 

@@ -112,6 +112,11 @@ cudaError_t launch_sum(float2 *out, const float2 *const *ins, int count, float p
                        cudaStream_t s);
 cudaError_t launch_min_max(const float2 *level0, const int32_t dims[3], int mips, float2 *levels, cudaStream_t s);
 
+/* DAS with its partial sums and tables in static device arrays (no allocation);
+ * capacity in float2 partial-sum entries (groups x voxels) */
+cudaError_t launch_das_no_alloc(DasParams p, const float4 *focal4, const int16_t *sparse, cudaStream_t s);
+int64_t     das_no_alloc_capacity();
+
 /* kernel launches issued since load (all launchers count here) */
 extern uint64_t g_kernel_launches;
 

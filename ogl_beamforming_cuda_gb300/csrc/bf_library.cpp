@@ -1052,6 +1052,89 @@ LIB_FN uint32_t beamformer_gb300_set_interpolation(int32_t mode)
 	return 1;
 }
 
+/* See include/ogl_beamformer_lib.h. Allocates nothing: no cudaMalloc, no
+ * cudaFree, no allocating library call; the partial sums and the focal/sparse
+ * tables live in static device arrays of bf_das.cu. Divisions and square roots
+ * take the IEEE path, which the allocated path's faster forms equal bit for bit. */
+LIB_FN uint32_t beamformer_gb300_das_no_alloc(const BeamformerParameters *das_parameters, const float *focal_vectors,
+                                              const int16_t *sparse_elements, const void *channel_data,
+                                              uint64_t channel_data_bytes, float *frame, void *cuda_stream)
+{
+	if (!das_parameters || !channel_data || !frame) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	int ndev = 0;
+	if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+		cudaGetLastError();
+		return fail(BF_LIB_ERR_KIND_CUDA_DEVICE);
+	}
+	const BeamformerParameters &d = *das_parameters;
+	DasParams p{};
+	for (int i = 0; i < 3; i++) p.dims[i] = d.output_points[i] > 1 ? d.output_points[i] : 1;
+	p.S = (int32_t)d.dec_data_dim[0];
+	p.C = (int32_t)d.dec_data_dim[1];
+	p.T = (int32_t)d.dec_data_dim[2];
+	const int64_t dense = (int64_t)p.C * p.T * p.S;
+	const int64_t have = (int64_t)(channel_data_bytes / sizeof(float2));
+	p.rf = (const float2 *)channel_data;
+	p.rf_count = have < dense ? have : dense;
+	p.frame = (float2 *)frame;
+	voxel_transform(d, p.M);
+	std::memcpy(p.X, d.xdc_transform, sizeof(p.X));
+	p.das_id = (int32_t)d.das_shader_id;
+	switch (d.das_shader_id) {
+	case DASShaderKind_FORCES: case DASShaderKind_UFORCES:       p.family = DAS_FORCES; break;
+	case DASShaderKind_HERCULES: case DASShaderKind_UHERCULES:   p.family = DAS_HERCULES; break;
+	case DASShaderKind_RCA_VLS: case DASShaderKind_RCA_TPW:
+	case DASShaderKind_FLASH:                                     p.family = DAS_RCA; break;
+	default:                                                      p.family = DAS_NONE; break;
+	}
+	p.sparse_mode = d.das_shader_id == DASShaderKind_UFORCES || d.das_shader_id == DASShaderKind_UHERCULES;
+	p.fast = !d.coherency_weighting;
+	p.coherency = d.coherency_weighting != 0;
+	p.interp = d.interpolate ? INTERP_CUBIC : INTERP_NEAREST;
+	p.tx_rows = !((d.transmit_mode & 2) != 0);
+	p.rx_cols = (d.transmit_mode & 1) != 0;
+	p.rx_rows = !p.rx_cols;
+	p.loop_end = (d.das_shader_id == DASShaderKind_RCA_VLS || d.das_shader_id == DASShaderKind_RCA_TPW) ? p.T : p.C;
+	p.fs = d.sampling_frequency;
+	p.fc = d.center_frequency;
+	p.c = d.speed_of_sound;
+	p.toff = d.time_offset;
+	const float r360 = 360.0f * DEG2RAD_F;
+	p.r360_fc = r360 * d.center_frequency;
+	p.apod_scale = d.f_number * (180.0f * DEG2RAD_F);
+	p.apod_hi = 0.25f * r360;
+	p.inv_sqrt_T = 1.0f / sqrtf((float)p.T);
+	p.px = d.xdc_element_pitch[0];
+	p.py = d.xdc_element_pitch[1];
+	p.cy_forces = p.py * (float)(p.C / 2);
+	p.rc = 1.0f / p.c;
+	p.rfs = 1.0f / p.fs;
+	p.c_lo = p.fs_lo = INFINITY;
+	p.c_hi = p.fs_hi = 0.0f;
+	p.fast_sqrt = 0;
+	p.dense_rows = p.rf_count >= dense && dense < (1ll << 31) && p.S >= 4;
+	p.groups = 1;
+	p.per_group = p.loop_end;
+	const int64_t vblocks = (int64_t)((p.dims[0] + 7) / 8) * p.dims[1] * ((p.dims[2] + 15) / 16);
+	if (p.fast && p.loop_end > 1 && vblocks < 2048) {
+		int64_t want = (2048 + vblocks - 1) / vblocks;
+		if (want > p.loop_end) want = p.loop_end;
+		p.per_group = (int32_t)((p.loop_end + want - 1) / want);
+		p.groups = (p.loop_end + p.per_group - 1) / p.per_group;
+	}
+	const int64_t nv = (int64_t)p.dims[0] * p.dims[1] * p.dims[2];
+	if (p.groups > 1 && (int64_t)p.groups * nv > das_no_alloc_capacity()) return fail(BF_LIB_ERR_KIND_BUFFER_OVERFLOW);
+	float4 focal[256];
+	for (int i = 0; i < 256; i++) {
+		const float angle = focal_vectors ? focal_vectors[2 * i] * DEG2RAD_F : 0.0f;
+		const float depth = focal_vectors ? focal_vectors[2 * i + 1] : 0.0f;
+		focal[i] = make_float4(sinf(angle), cosf(angle), depth, std::isinf(depth) ? 1.0f : 0.0f);
+	}
+	int16_t sparse[256];
+	for (int i = 0; i < 256; i++) sparse[i] = sparse_elements ? sparse_elements[i] : (int16_t)i;
+	return cuda_ok(launch_das_no_alloc(p, focal, sparse, (cudaStream_t)cuda_stream)) ? 1 : 0;
+}
+
 LIB_FN uint64_t beamformer_gb300_kernel_launch_count(void) { return g_kernel_launches; }
 
 LIB_FN void beamformer_gb300_shutdown(void)
