@@ -108,6 +108,12 @@ cudaError_t launch_verify_division(float b, float rb, float lo, float hi, unsign
 cudaError_t launch_decode(const DecodeParams &p, cudaStream_t s);
 cudaError_t launch_filter(const FilterParams &p, cudaStream_t s);
 cudaError_t launch_das(const DasParams &p, cudaStream_t s);
+cudaError_t launch_das_reduce(const float2 *partial, float2 *frame, int64_t n, int groups, cudaStream_t s);
+/* HERCULES fast path (bf_das_hercules.cu): for parameters das_hercules_supported
+ * accepts; `table` holds das_hercules_table_entries float4 (none for nearest) */
+bool        das_hercules_supported(const DasParams &p);
+int64_t     das_hercules_table_entries(const DasParams &p);
+cudaError_t launch_das_hercules(const DasParams &p, float4 *table, cudaStream_t s);
 cudaError_t launch_sum(float2 *out, const float2 *const *ins, int count, float prescale, const int32_t dims[3],
                        cudaStream_t s);
 cudaError_t launch_min_max(const float2 *level0, const int32_t dims[3], int mips, float2 *levels, cudaStream_t s);

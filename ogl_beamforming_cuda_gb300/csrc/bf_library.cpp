@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <thread>
 #include <vector>
@@ -124,6 +125,8 @@ struct Context {
 	/* DAS: partial sums of channel groups, and verified division ranges per divisor */
 	float2      *das_partial = nullptr;
 	uint64_t     das_partial_bytes = 0;
+	float4      *das_table = nullptr;         /* HERCULES interpolation table */
+	uint64_t     das_table_bytes = 0;
 	unsigned long long *d_mismatch = nullptr;
 	struct DivCheck { float b, lo, hi; };
 	std::vector<DivCheck> div_checks;
@@ -593,12 +596,13 @@ bool run_stage(int i, const void *src, uint64_t src_bytes, DeviceFrame &frame, b
 		p.sparse = g.d_sparse;
 		p.rc = 1.0f / p.c;
 		p.rfs = 1.0f / p.fs;
-		/* distances from 61 um to 8 m, sample indices from 1/256 to 65536 */
-		if (!division_range(p.c, 0x1p-14f, 8.0f, p.c_lo, p.c_hi)) return false;
-		if (!division_range(p.fs, 0x1p-8f, 65536.0f, p.fs_lo, p.fs_hi)) return false;
+		/* distances and sample indices in [2^-100, 2^20] (below, the quotients by
+		 * c and fs would be subnormal) */
+		if (!division_range(p.c, 0x1p-100f, 0x1p20f, p.c_lo, p.c_hi)) return false;
+		if (!division_range(p.fs, 0x1p-100f, 0x1p20f, p.fs_lo, p.fs_hi)) return false;
 		p.fast_sqrt = sqrt_verified() ? 1 : 0;
-		p.sqrt_lo = 0x1p-40f;
-		p.sqrt_hi = 0x1p24f;
+		p.sqrt_lo = 0x1p-100f;
+		p.sqrt_hi = 0x1p30f;
 		{
 			const int64_t dense = (int64_t)p.C * p.T * p.S;
 			p.dense_rows = p.rf_count >= dense && dense < (1ll << 31) && p.S >= 4;
@@ -626,7 +630,22 @@ bool run_stage(int i, const void *src, uint64_t src_bytes, DeviceFrame &frame, b
 			}
 			p.partial = g.das_partial;
 		}
-		err = launch_das(p, g.stream);
+		/* OGL_BF_DAS_GENERIC=1 keeps every DAS on das_kernel (for comparisons) */
+		const char *generic = std::getenv("OGL_BF_DAS_GENERIC");
+		if (das_hercules_supported(p) && !(generic && generic[0] == '1')) {
+			const uint64_t need = (uint64_t)das_hercules_table_entries(p) * sizeof(float4);
+			if (need > g.das_table_bytes) {
+				cudaStreamSynchronize(g.stream);
+				cudaFree(g.das_table);
+				g.das_table = nullptr;
+				g.das_table_bytes = 0;
+				if (!cuda_ok(cudaMalloc(&g.das_table, need))) return false;
+				g.das_table_bytes = need;
+			}
+			err = launch_das_hercules(p, g.das_table, g.stream);
+		} else {
+			err = launch_das(p, g.stream);
+		}
 		frame.written = true;
 	} break;
 	case BeamformerShaderKind_Sum: {
@@ -1154,6 +1173,7 @@ LIB_FN void beamformer_gb300_shutdown(void)
 	cudaFree(g.chan[0]); cudaFree(g.chan[1]);
 	cudaFree(g.hadamard);
 	cudaFree(g.das_partial);
+	cudaFree(g.das_table);
 	cudaFree(g.d_mismatch);
 	cudaFree(g.d_chmap); cudaFree(g.d_sparse); cudaFree(g.d_focal);
 	for (auto &st : g.stage_tables) { cudaFree(st.taps); cudaFree(st.phasor); }

@@ -118,6 +118,26 @@ def test_das_modes(das, interp, coh):
     check_volume(vol, ref["frame"], f"DAS {das} interp={interp} coherency={coh}")
 
 
+@pytest.mark.parametrize("interp", (0, 1, 2))
+@pytest.mark.parametrize("points", ((16, 3, 20), (40, 1, 48)))
+def test_das_hercules_generic_kernel(monkeypatch, interp, points):
+    """HERCULES volumes normally take the dedicated kernel; the general kernel
+    (OGL_BF_DAS_GENERIC=1) must agree with the oracle too."""
+    monkeypatch.setenv("OGL_BF_DAS_GENERIC", "1")
+    bp = small_params(S=512, C=16, T=16, points=points)
+    raw = small_raw(bp)
+    bf, ref = run_both(bp, [SH["Decode"], SH["Demodulate"], SH["DAS"]], raw, interpolation=interp)
+    check_volume(bf.frame(0)[0], ref["frame"], f"HERCULES general kernel interp={interp}")
+
+
+@pytest.mark.parametrize("interp", (0, 1, 2))
+def test_das_hercules_plane_32_channels(interp):
+    bp = small_params(S=1024, C=32, T=32, points=(48, 1, 64), D=2)
+    raw = small_raw(bp, n_points=12, n_speckle=200)
+    bf, ref = run_both(bp, [SH["Decode"], SH["Demodulate"], SH["DASFast"]], raw, interpolation=interp)
+    check_volume(bf.frame(0)[0], ref["frame"], f"HERCULES DASFast 32x32 interp={interp}")
+
+
 def test_das_unknown_kind_is_zero():
     bp = small_params(S=512, C=16, T=16, das="RACES")
     raw = small_raw(bp)
