@@ -39,6 +39,8 @@ FILTER_TAPS = 64
 N_POINTS, N_SPECKLE = 200, 20000
 METRIC = "volumes/s plain vs mixed-precision/learned pipeline at NRMSE <= -40 dB, 1 GB300"
 DAS_FLOPS_PER_TERM = 40            # cubic sample-op: interpolation, apodization, phase rotation, accumulate
+DAS_BYTES_PER_TERM = 32            # cubic sample-op: four complex f32 samples read from L1/shared memory
+L1_BYTES_PER_CLK_SM = 128          # L1/shared-memory data path per SM per clock
 
 
 def parse():
@@ -49,18 +51,41 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--speckle", type=int, default=N_SPECKLE)
+    ap.add_argument("--profile-frames", type=int, default=0,
+                    help="only push this many copies of one device-resident frame through the pipeline "
+                         "(for a profiler), print per-stage ms and exit")
+    ap.add_argument("--points", default=",".join(map(str, POINTS)), help="voxel grid for --profile-frames")
     return ap.parse_args()
 
 
-def workload():
+def workload(points=POINTS):
     from ogl_beamforming_cuda_gb300 import synth
-    bp = synth.make_parameters(samples=S, channels=C, transmits=T, points=POINTS, decimation=2, f_number=1.0,
+    bp = synth.make_parameters(samples=S, channels=C, transmits=T, points=points, decimation=2, f_number=1.0,
                                interpolate=1, frames=FRAMES, filter_length=FILTER_TAPS)
     return bp, synth.default_pipeline(sum_and_minmax=True), synth.kaiser_spec(FILTER_TAPS)
 
 
+def profile_frames(args):
+    """The workload's pipeline on one seeded frame pushed args.profile_frames times."""
+    import torch
+    from ogl_beamforming_cuda_gb300 import synth
+    from ogl_beamforming_cuda_gb300.client import Beamformer
+    torch.cuda.set_device(0)
+    points = tuple(int(v) for v in args.points.split(","))
+    bp, pipe, kaiser = workload(points)
+    bf = Beamformer().configure(bp, pipe, kaiser=kaiser)
+    raw = torch.from_numpy(synth.acquisition(bp, 1000, n_points=N_POINTS, n_speckle=args.speckle, device="cuda:0"))
+    raw = raw.to("cuda:0")
+    for _ in range(args.profile_frames):
+        bf.push_device(raw.data_ptr(), raw.numel() * 2)
+    bf.synchronize()
+    print(json.dumps({"points": points, "frames": args.profile_frames,
+                      "stage_ms": {k: v * 1e3 for k, v in stage_times(bf, args.profile_frames).items()}}))
+    return 0
+
+
 def config_dict(extra=None):
-    d = {"workload": "HERCULES RCA 128+128, 128 tx, 2048 samples int16 -> decode -> demod(64 taps, /4) -> "
+    d = {"workload": "HERCULES RCA 128+128, 128 tx, 2048 samples int16 -> decode -> demod(64 taps, IQ pairs, decimation 2: 512 samples) -> "
                      "cubic DAS 128x128x256 -> 16-frame sum -> min_max",
          "frames_per_volume": FRAMES, "voxels": int(np.prod(POINTS)), "transmits": T, "channels": C,
          "samples": S, "interpolation": "cubic", "scatterers": N_POINTS, "speckle_scatterers": N_SPECKLE,
@@ -165,6 +190,37 @@ def fp32_peak_tflops(peaks):
     MEASURED_PEAKS.json carries no FP32 figure, so the measured max clock is used."""
     mhz = float(peaks.get("sm_max_mhz", 2070.0))
     return 152 * 128 * 2 * mhz * 1e6 / 1e12
+
+
+def l1_peak_gbs(peaks):
+    """Nominal L1/shared-memory bandwidth: 152 SMs x 128 B x max SM clock."""
+    mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    return 152 * L1_BYTES_PER_CLK_SM * mhz * 1e6 / 1e9
+
+
+def das_roofline(das_t, peaks, traffic):
+    """DAS is bound by min(FP32 peak / 40 flops, L1 bandwidth / 32 B) per cubic
+    sample-op (one (voxel, transmit, receive) term); for cubic the L1 term is the
+    smaller, so the roofline is stated in L1 bytes."""
+    ops = int(np.prod(POINTS)) * T * C
+    fp32 = fp32_peak_tflops(peaks)
+    l1 = l1_peak_gbs(peaks)
+    ops_fp32, ops_l1 = fp32 * 1e12 / DAS_FLOPS_PER_TERM, l1 * 1e9 / DAS_BYTES_PER_TERM
+    out = {"kernel": "das_hercules<cubic> (+ its interpolation-table pass)", "sample_ops_per_launch": ops,
+           "bytes_per_sample_op": DAS_BYTES_PER_TERM, "flops_per_sample_op": DAS_FLOPS_PER_TERM,
+           "peak_source": "nominal from sm_max_mhz of MEASURED_PEAKS.json (it holds no L1 or FP32 figure): "
+                          "L1 152 x 128 B/clk, FP32 152 x 128 x 2 flop/clk",
+           "traffic": traffic, "das_ms": das_t * 1e3 if das_t else None}
+    if ops_l1 <= ops_fp32:
+        out.update(bound="l1", unit="GB/s", peak=l1,
+                   achieved=ops * DAS_BYTES_PER_TERM / das_t / 1e9 if das_t else None)
+    else:
+        out.update(bound="fp32", unit="TFLOP/s", peak=fp32,
+                   achieved=ops * DAS_FLOPS_PER_TERM / das_t / 1e12 if das_t else None)
+    out["frac"] = out["achieved"] / out["peak"] if das_t else None
+    out["fp32_tflops"] = ops * DAS_FLOPS_PER_TERM / das_t / 1e12 if das_t else None
+    out["fp32_frac"] = out["fp32_tflops"] / fp32 if das_t else None
+    return out
 
 
 def run_ours(args, rank, world, local, dist):
@@ -296,6 +352,8 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     peaks = measured_peaks()
+    if args.profile_frames > 0:
+        return profile_frames(args)
 
     if args.impl == "reference":
         if rank != 0:
@@ -332,10 +390,6 @@ def main():
     e2e = args.steps * world / r["te"]
     st = r["stages"]
     das_t = st.get("DASFast") or st.get("DAS")
-    V = int(np.prod(POINTS))
-    flops = V * T * C * DAS_FLOPS_PER_TERM
-    peak = fp32_peak_tflops(peaks)
-    achieved = flops / das_t / 1e12 if das_t else None
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     stage_roof = {}
     for k, b in algorithmic_bytes().items():
@@ -354,11 +408,7 @@ def main():
         "e2e": {"value": e2e, "unit": "volumes/s", "h2d_bytes_per_step": FRAMES * r["nbytes"],
                 "d2h_bytes_per_step": r["out_bytes"]},
         "gpu_launches": r["launches"],
-        "roofline": {"kernel": "das_kernel<HERCULES, cubic, fast>", "bound": "fp32", "achieved": achieved,
-                     "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
-                     "traffic": traffic, "algorithmic_flops_per_launch": flops,
-                     "peak_source": "nominal FP32 (152 SMs x 128 lanes x 2 x sm_max_mhz of MEASURED_PEAKS.json)",
-                     "das_ms": das_t * 1e3 if das_t else None},
+        "roofline": das_roofline(das_t, peaks, traffic),
         "stages": stage_roof,
         "clocks": r["clocks"],
     }
