@@ -320,19 +320,24 @@ def cpu_sample(budget_s=12.0):
     sparse = np.arange(256, dtype=np.int16)
     V = int(np.prod(POINTS))
     frame = np.zeros(2 * V, np.float32)
+    # stratified random runs of voxels: one run per stratum of V / ranges voxels,
+    # so shallow and deep, central and edge voxels (whose active aperture differs)
+    # are all represented
     ranges = 16
-    per = 64
-    t0 = time.perf_counter()
-    for i in range(ranges):
-        v0 = (V // ranges) * i + V // (2 * ranges)
-        O.das(plan.das, rf, POINTS, sparse, focal, fast=True, voxel_begin=v0, voxel_end=v0 + per, out=frame)
-    probe = time.perf_counter() - t0
-    per = int(max(64, min(V // ranges, per * (0.6 * budget_s) / max(probe, 1e-3))))
-    t0 = time.perf_counter()
-    for i in range(ranges):
-        v0 = (V // ranges) * i + V // (2 * ranges) - per // 2
-        O.das(plan.das, rf, POINTS, sparse, focal, fast=True, voxel_begin=v0, voxel_end=v0 + per, out=frame)
-    t_das = (time.perf_counter() - t0) * V / (ranges * per)
+    srng = np.random.default_rng(1)
+    stratum = V // ranges
+
+    def das_runs(per):
+        t0 = time.perf_counter()
+        for i in range(ranges):
+            v0 = stratum * i + int(srng.integers(0, max(1, stratum - per)))
+            O.das(plan.das, rf, POINTS, sparse, focal, fast=True, voxel_begin=v0, voxel_end=v0 + per, out=frame)
+        return time.perf_counter() - t0
+
+    per = 256           # long enough runs for the oracle's threads to share evenly
+    probe = das_runs(per)
+    per = int(max(256, min(stratum, per * (0.6 * budget_s) / max(probe, 1e-3))))
+    t_das = das_runs(per) * V / (ranges * per)
 
     frames = [np.zeros(2 * V, np.float32) for _ in range(FRAMES)]
     t0 = time.perf_counter()
@@ -340,7 +345,8 @@ def cpu_sample(budget_s=12.0):
     O.min_max(frames[0], POINTS)
     t_tail = time.perf_counter() - t0
     t_volume = FRAMES * (t_front + t_das + t_tail)
-    sample = (f"decode+demod of {csub}/{C} channels, DAS of {ranges * per}/{V} voxels in {ranges} ranges, "
+    sample = (f"decode+demod of {csub}/{C} channels, DAS of {ranges * per}/{V} voxels in {ranges} stratified "
+              f"random runs, "
               f"full sum+min_max; scaled to {FRAMES} frames (extrapolated)")
     return {"value": 1.0 / t_volume, "unit": "volumes/s", "cores": threads, "kind": "port", "sample": sample,
             "seconds_per_volume": t_volume}
