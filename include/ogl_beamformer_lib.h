@@ -329,6 +329,16 @@ LIB_FN uint32_t beamformer_gb300_get_filter(uint8_t slot, float *taps, int32_t c
  * Linear interpolation has no counterpart in the reference. */
 LIB_FN uint32_t beamformer_gb300_set_interpolation(int32_t mode);
 
+/* Arithmetic of the front end (no counterpart in the reference; the precision
+ * variant): 0 = FP32 as the reference (default); 1 = FP16, 2 = BF16. With 1 or 2
+ * a pipeline must start Decode (int16 data, Hadamard order a power of two <= 128)
+ * -> Demodulate with decimation 1, 2 or 4 and at most 160 taps: the decoded
+ * samples are rounded once to the 16-bit type, and the demodulating FIR runs as
+ * a Toeplitz contraction on the tensor cores with FP32 accumulation. DAS and the
+ * later stages stay FP32. Other pipelines fail with UNSUPPORTED at compute time
+ * while a 16-bit precision is selected. Takes effect at the next compute. */
+LIB_FN uint32_t beamformer_gb300_set_filter_precision(int32_t precision);
+
 /* Delay-and-sum of one frame that allocates no device memory. Has no
  * counterpart in the reference. It is meant for callers that cannot let a
  * library allocate on the GPU while they run: for example an acquisition loop

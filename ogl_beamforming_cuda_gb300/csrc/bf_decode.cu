@@ -22,6 +22,9 @@
  */
 #include "bf_kernels.h"
 
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 namespace bf {
 
 uint64_t g_kernel_launches = 0;
@@ -64,7 +67,20 @@ decode_fwht_i16(DecodeParams p)
 	fwht<N>(v);
 
 	const float inv_n = 1.0f / (float)N;   /* exact: N is a power of two */
-	if (p.output == DEC_OUT_REAL_PAIRS) {
+	if (p.output == DEC_OUT_REAL_F16 || p.output == DEC_OUT_REAL_BF16) {
+		/* real pairs layout, 16-bit elements: the value rounded once from the exact
+		 * f32 decode */
+		uint64_t pair = s >> 1;
+		uint16_t *o16 = (uint16_t *)p.out;
+		#pragma unroll
+		for (int t = 0; t < N; t++) {
+			uint64_t o = (uint64_t)p.st.out_channel * c + (uint64_t)p.st.out_transmit * t + (uint64_t)p.st.out_sample * pair;
+			const float y = __fmul_rn((float)v[t], inv_n);
+			if (o < p.out_vec2)
+				o16[2 * o + (s & 1)] = p.output == DEC_OUT_REAL_F16 ? __half_as_ushort(__float2half_rn(y))
+				                                                     : __bfloat16_as_ushort(__float2bfloat16_rn(y));
+		}
+	} else if (p.output == DEC_OUT_REAL_PAIRS) {
 		uint64_t pair = s >> 1;
 		#pragma unroll
 		for (int t = 0; t < N; t++) {
@@ -162,6 +178,7 @@ cudaError_t launch_decode(const DecodeParams &p, cudaStream_t s)
 			return cudaGetLastError();
 		}
 	}
+	if (p.output == DEC_OUT_REAL_F16 || p.output == DEC_OUT_REAL_BF16) return cudaErrorInvalidValue;
 	size_t smem = (size_t)p.transmits * 32 * sizeof(float2);
 	static bool attr_set = false;
 	if (!attr_set) {

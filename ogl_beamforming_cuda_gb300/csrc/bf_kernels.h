@@ -18,7 +18,9 @@ struct Strides {
 
 /* ------------------------------- decode ---------------------------------- */
 enum DecodeInput  { DEC_IN_I16 = 0, DEC_IN_I16C = 1, DEC_IN_F32 = 2, DEC_IN_F32C = 3 };
-enum DecodeOutput { DEC_OUT_COMPLEX = 0, DEC_OUT_REAL_PAIRS = 1 };
+/* REAL_F16 / REAL_BF16: the real pairs layout as 16-bit floats (the precision
+ * variant's input to the tensor-core FIR) */
+enum DecodeOutput { DEC_OUT_COMPLEX = 0, DEC_OUT_REAL_PAIRS = 1, DEC_OUT_REAL_F16 = 2, DEC_OUT_REAL_BF16 = 3 };
 
 struct DecodeParams {
 	const void    *in;             /* raw RF or previous stage output */
@@ -108,6 +110,17 @@ cudaError_t launch_verify_division(float b, float rb, float lo, float hi, unsign
 cudaError_t launch_decode(const DecodeParams &p, cudaStream_t s);
 cudaError_t launch_filter(const FilterParams &p, cudaStream_t s);
 cudaError_t launch_das(const DasParams &p, cudaStream_t s);
+/* Precision variant of DemodulateFloat after a 16-bit Decode (bf_fir_tc.cu):
+ * Toeplitz contraction on tcgen05 tensor cores, fp16/bf16 operands, f32
+ * accumulate. `table` (fir_tc_table_bytes, device) holds the tap matrix and the
+ * per-output rotations written by fir_tc_tables. */
+bool        fir_tc_supported(uint32_t decimation, uint32_t taps);
+int64_t     fir_tc_table_bytes(uint32_t decimation, uint32_t taps, uint32_t n_out);
+bool        fir_tc_tables(uint32_t decimation, const float *h, uint32_t taps, double demod_frequency,
+                          double demod_fs, uint32_t n_out, bool bf16, void *table);
+cudaError_t launch_fir_tc(const void *x, uint32_t rows, uint32_t row_samples, uint32_t valid_samples,
+                          uint32_t decimation, uint32_t taps, uint32_t n_out, bool bf16, const void *table,
+                          float2 *out, unsigned *error, cudaStream_t s);
 cudaError_t launch_das_reduce(const float2 *partial, float2 *frame, int64_t n, int groups, cudaStream_t s);
 /* HERCULES fast path (bf_das_hercules.cu): for parameters das_hercules_supported
  * accepts; `table` holds das_hercules_table_entries float4 (none for nearest) */

@@ -121,6 +121,13 @@ struct Context {
 	std::chrono::steady_clock::time_point last_upload{};
 	bool         have_last_upload = false;
 	int32_t      interpolation_override = -1;
+	/* precision variant: 0 FP32 (reference arithmetic), 1 FP16, 2 BF16 Decode output
+	 * and tensor-core Demodulate FIR */
+	int32_t      precision = 0;
+	bool         tc_active = false;
+	void        *tc_table = nullptr;
+	size_t       tc_table_cap = 0;
+	unsigned    *d_tc_error = nullptr;
 
 	/* DAS: partial sums of channel groups, and verified division ranges per divisor */
 	float2      *das_partial = nullptr;
@@ -227,6 +234,48 @@ bool ensure_frame(DeviceFrame &f, const int32_t dims[3])
 }
 
 /* (Re)build everything derived from the pushed state. */
+/* Precision variant: a first-stage int16 Hadamard Decode (fast Walsh-Hadamard
+ * orders) writing fp16/bf16, followed by DemodulateFloat on the tensor cores, with
+ * dense [channel][transmit][sample] layouts. Other pipelines fail UNSUPPORTED
+ * while a 16-bit precision is selected. */
+bool prepare_precision()
+{
+	g.tc_active = false;
+	if (g.precision == 0) return true;
+	const Plan &pl = g.plan;
+	const uint32_t T = pl.das.dec_data_dim[2], C = pl.das.dec_data_dim[1];
+	bool ok = pl.count >= 2 && pl.shaders[0] == BeamformerShaderKind_DecodeInt16ToFloat &&
+	          pl.shaders[1] == BeamformerShaderKind_DemodulateFloat && g.data_kind == BeamformerDataKind_Int16 &&
+	          pl.decode_mode == DECODE_MODE_HADAMARD && g.hadamard_ok && g.hadamard_base == 1 &&
+	          (uint32_t)g.hadamard_sylvester == pl.transmit_count && pl.transmit_count <= 128;
+	const Strides &ds = pl.decode_st, &ms = pl.demod_st;
+	const std::vector<float> &h = g.taps[pl.slots[1] % BEAMFORMER_FILTER_SLOTS];
+	const uint32_t L = (uint32_t)h.size(), D = pl.demod_decimation, n_out = ms.out_transmit;
+	ok = ok && ds.out_sample == 1 && ds.out_channel == (uint64_t)ds.out_transmit * T && ms.in_sample == 1 &&
+	     ms.in_transmit == ds.out_transmit && ms.in_channel == ds.out_channel && ms.out_sample == 1 &&
+	     ms.out_channel == (uint64_t)n_out * T && (2 * ds.out_transmit) % 8 == 0 && n_out > 0 &&
+	     (uint64_t)C * T * n_out * 8 <= g.chan_bytes && fir_tc_supported(D, L);
+	if (!ok) return fail(BF_LIB_ERR_KIND_UNSUPPORTED), false;
+	const size_t need = (size_t)fir_tc_table_bytes(D, L, n_out);
+	if (need > g.tc_table_cap) {
+		cudaStreamSynchronize(g.stream);
+		cudaFree(g.tc_table);
+		g.tc_table = nullptr;
+		g.tc_table_cap = 0;
+		if (!cuda_ok(cudaMalloc(&g.tc_table, need))) return false;
+		g.tc_table_cap = need;
+	}
+	if (!g.d_tc_error) {
+		if (!cuda_ok(cudaMalloc(&g.d_tc_error, sizeof(unsigned)))) return false;
+		if (!cuda_ok(cudaMemset(g.d_tc_error, 0, sizeof(unsigned)))) return false;
+	}
+	cudaStreamSynchronize(g.stream);
+	if (!fir_tc_tables(D, h.data(), L, pl.demod_frequency, pl.demod_fs, n_out, g.precision == 2, g.tc_table))
+		return fail(BF_LIB_ERR_KIND_CUDA_RUNTIME), false;
+	g.tc_active = true;
+	return true;
+}
+
 bool prepare()
 {
 	if (!g.dirty && g.plan_ok) return true;
@@ -277,6 +326,8 @@ bool prepare()
 		}
 		g.hadamard_order = order;
 	}
+	if (!prepare_precision()) return false;
+
 	bool uses_decode = false;
 	for (int i = 0; i < pl.count; i++)
 		if (pl.shaders[i] == BeamformerShaderKind_Decode || pl.shaders[i] == BeamformerShaderKind_DecodeInt16Complex ||
@@ -499,12 +550,13 @@ bool run_stage(int i, const void *src, uint64_t src_bytes, DeviceFrame &frame, b
 		p.hadamard = g.hadamard;
 		p.st = pl.decode_st;
 		p.output = kind == BeamformerShaderKind_DecodeInt16ToFloat ? DEC_OUT_REAL_PAIRS : DEC_OUT_COMPLEX;
+		if (g.tc_active && i == 0) p.output = g.precision == 2 ? DEC_OUT_REAL_BF16 : DEC_OUT_REAL_F16;
 		/* samples the reference's dispatch writes: pass-2 guard (time sample < output
 		 * transmit stride) and grid width; int16 data decoded first packs two samples
 		 * per invocation */
 		const uint32_t ots = pl.decode_st.out_transmit, cov = pl.decode_invocations_x;
 		const bool pairs = first && g.data_kind == BeamformerDataKind_Int16;
-		if (p.output == DEC_OUT_REAL_PAIRS)
+		if (p.output == DEC_OUT_REAL_PAIRS || p.output == DEC_OUT_REAL_F16 || p.output == DEC_OUT_REAL_BF16)
 			p.samples = 2 * std::min(ots, cov);
 		else if (pairs)
 			p.samples = 2 * std::min((ots + 1) / 2, cov);
@@ -523,6 +575,17 @@ bool run_stage(int i, const void *src, uint64_t src_bytes, DeviceFrame &frame, b
 	case BeamformerShaderKind_Demodulate:
 	case BeamformerShaderKind_DemodulateFloat:
 	case BeamformerShaderKind_Filter: {
+		if (g.tc_active && i == 1) {
+			const Strides &ds = pl.decode_st;
+			const uint32_t rows = pl.das.dec_data_dim[1] * pl.das.dec_data_dim[2];
+			const uint32_t valid = 2 * std::min(ds.out_transmit, pl.decode_invocations_x);
+			const uint32_t L = (uint32_t)g.taps[pl.slots[i] % BEAMFORMER_FILTER_SLOTS].size();
+			err = launch_fir_tc(g.chan[in_idx], rows, 2 * ds.out_transmit, valid, pl.demod_decimation, L,
+			                    pl.demod_st.out_transmit, g.precision == 2, g.tc_table, (float2 *)g.chan[out_idx],
+			                    g.d_tc_error, g.stream);
+			g.last_chan = out_idx;
+			break;
+		}
 		FilterParams p{};
 		const bool is_filter = kind == BeamformerShaderKind_Filter;
 		const bool map = !is_filter && pl.demod_map;
@@ -1014,7 +1077,17 @@ LIB_FN uint32_t beamformer_gb300_synchronize(int32_t timeout_ms)
 {
 	if (!g.ready) return 1;
 	if (!wait_event(g.last_done, timeout_ms)) return fail(BF_LIB_ERR_KIND_SYNC_VARIABLE);
-	return cuda_ok(cudaStreamSynchronize(g.stream)) ? 1 : 0;
+	if (!cuda_ok(cudaStreamSynchronize(g.stream))) return 0;
+	if (g.d_tc_error) {
+		/* a tensor-core FIR wait that ran out (the kernel stopped early) */
+		unsigned e = 0;
+		if (!cuda_ok(cudaMemcpy(&e, g.d_tc_error, sizeof(e), cudaMemcpyDeviceToHost))) return 0;
+		if (e) {
+			cudaMemset(g.d_tc_error, 0, sizeof(unsigned));
+			return fail(BF_LIB_ERR_KIND_CUDA_RUNTIME);
+		}
+	}
+	return 1;
 }
 
 LIB_FN uint32_t beamformer_gb300_export_frame(uint32_t which, uint32_t mip_level, float *out, uint64_t out_size,
@@ -1061,6 +1134,16 @@ LIB_FN uint32_t beamformer_gb300_get_filter(uint8_t slot, float *taps, int32_t c
 	if (!taps) return 1;
 	if (capacity < n) return fail(BF_LIB_ERR_KIND_BUFFER_OVERFLOW);
 	std::memcpy(taps, g.taps[s].data(), (size_t)n * sizeof(float));
+	return 1;
+}
+
+LIB_FN uint32_t beamformer_gb300_set_filter_precision(int32_t precision)
+{
+	if (precision < 0 || precision > 2) return fail(BF_LIB_ERR_KIND_UNSUPPORTED);
+	if (precision != g.precision) {
+		g.precision = precision;
+		g.dirty = true;
+	}
 	return 1;
 }
 
@@ -1174,6 +1257,8 @@ LIB_FN void beamformer_gb300_shutdown(void)
 	cudaFree(g.hadamard);
 	cudaFree(g.das_partial);
 	cudaFree(g.das_table);
+	cudaFree(g.tc_table);
+	cudaFree(g.d_tc_error);
 	cudaFree(g.d_mismatch);
 	cudaFree(g.d_chmap); cudaFree(g.d_sparse); cudaFree(g.d_focal);
 	for (auto &st : g.stage_tables) { cudaFree(st.taps); cudaFree(st.phasor); }
@@ -1192,6 +1277,7 @@ LIB_FN void beamformer_gb300_shutdown(void)
 	for (int i = 0; i < BEAMFORMER_FILTER_SLOTS; i++) { fresh.filters[i] = g.filters[i]; fresh.taps[i] = g.taps[i]; }
 	fresh.timeout_ms = g.timeout_ms;
 	fresh.interpolation_override = g.interpolation_override;
+	fresh.precision = g.precision;
 	g = fresh;
 }
 

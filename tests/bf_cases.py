@@ -68,3 +68,23 @@ def check_volume(vol, ref, what=""):
     assert db <= NRMSE_DB, f"{what}: NRMSE {db:.1f} dB > {NRMSE_DB} dB"
     assert float(np.max(np.abs(np.asarray(vol) - ref))) <= MAXABS_FRAC * max(peak, 1e-30), f"{what}: max-abs"
     return db
+
+
+def fp64_front_end(ref, kaiser, data_channels):
+    """FP64 restatement of the Demodulate stage on the oracle's (exact) decoded
+    samples: complex channel data of the stage's output region, float64 pairs."""
+    import ctypes
+    import oracle.bf_oracle as O
+    p = ref["plan"]
+    dec = ref["stages"][0][1].astype(np.float64)
+    out = np.zeros_like(dec)
+    taps = O.kaiser_f64(kaiser[1], kaiser[2], kaiser[0], kaiser[3])
+    O.lib().bfo_filter_f64(ctypes.byref(p.demod), abi.SHADER["DemodulateFloat"], O._ptr(dec), dec.size, O._ptr(out),
+                           out.size, O._arr(taps, ctypes.c_double), kaiser[3], p.demod_dispatch, O.threads())
+    n = 2 * int(p.demod.output_channel_stride) * data_channels
+    return out, n
+
+
+def nrmse(a, b):
+    from conftest import nrmse_db
+    return nrmse_db(a, b)

@@ -192,3 +192,11 @@ def test_no_device_fails_loudly(lib):
     assert lib.beamformer_push_data(raw.ctypes.data_as(ctypes.c_void_p), raw.nbytes) == 0
     assert lib.beamformer_get_last_error() == abi.ERR["CUDA_DEVICE"]
     assert lib.beamformer_start_compute() == 0
+
+
+def test_filter_precision_argument_checks(lib):
+    assert lib.beamformer_gb300_set_filter_precision(3) == 0
+    assert lib.beamformer_get_last_error() == abi.ERR["UNSUPPORTED"]
+    assert lib.beamformer_gb300_set_filter_precision(-1) == 0
+    for p in (1, 2, 0):
+        assert lib.beamformer_gb300_set_filter_precision(p) == 1
