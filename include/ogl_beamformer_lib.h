@@ -339,6 +339,32 @@ LIB_FN uint32_t beamformer_gb300_set_interpolation(int32_t mode);
  * while a 16-bit precision is selected. Takes effect at the next compute. */
 LIB_FN uint32_t beamformer_gb300_set_filter_precision(int32_t precision);
 
+/* Beamform `count` acquisitions in one go (the batched variant; no counterpart
+ * in the reference, which beamforms one acquisition per compute). Acquisition i
+ * has its own parameters[i] (transmit and sample counts, output grid, DAS mode),
+ * its raw RF at the DEVICE pointer rf[i] (rf_size[i] bytes, the pushed data kind)
+ * and its volume written to the DEVICE pointer out[i] (output_points x 2 floats,
+ * x fastest). All share the pushed pipeline, filters, channel mapping, sparse
+ * elements, focal vectors and interpolation; the pipeline's last stage must be DAS
+ * without coherency weighting, the DAS modes HERCULES (not sparse) or FORCES, and
+ * all acquisitions must use one interpolation mode. The front ends run per
+ * acquisition and the DAS of all acquisitions runs as one persistent launch; on
+ * the first call for a set of parameters and pointers the tile shape and grid
+ * size are autotuned on the device and the whole batch is captured in a CUDA graph,
+ * which later calls with the same set replay. timeout_ms as
+ * beamform_data_synchronized. Fails with UNSUPPORTED for other pipelines or a
+ * 16-bit filter precision. */
+LIB_FN uint32_t beamformer_gb300_beamform_batch(const BeamformerParameters *parameters, uint32_t count,
+                                                const void *const *rf, const uint64_t *rf_size, float *const *out,
+                                                int32_t timeout_ms);
+
+/* The autotuner's choice for the current batch: *volume_tiles 1 when HERCULES
+ * volumes use 4x4x16 voxel tiles (0: 8x1x16), *ctas the persistent grid size, and
+ * the timed DAS milliseconds of every candidate (tile shape x {4, 5, 6} CTAs per
+ * SM, in that order) when candidate_ms has room for *count_out values. */
+LIB_FN uint32_t beamformer_gb300_batch_tuning(int32_t *volume_tiles, int32_t *ctas, float *candidate_ms,
+                                              int32_t capacity, int32_t *count_out);
+
 /* Delay-and-sum of one frame that allocates no device memory. Has no
  * counterpart in the reference. It is meant for callers that cannot let a
  * library allocate on the GPU while they run: for example an acquisition loop

@@ -111,3 +111,22 @@ class Beamformer:
 
     def launches(self):
         return int(self.lib.beamformer_gb300_kernel_launch_count())
+
+    def beamform_batch(self, params, rf_ptrs, rf_sizes, out_ptrs, timeout_ms=-1):
+        """beamformer_gb300_beamform_batch over device buffers (integer addresses)."""
+        n = len(params)
+        arr = (abi.BeamformerParameters * n)(*params)
+        rf = (ctypes.c_void_p * n)(*rf_ptrs)
+        sz = (ctypes.c_uint64 * n)(*rf_sizes)
+        out = (ctypes.c_void_p * n)(*out_ptrs)
+        self._check(self.lib.beamformer_gb300_beamform_batch(arr, n, rf, sz, out, timeout_ms), "beamform_batch")
+
+    def batch_tuning(self):
+        """(volume tiles, persistent CTAs, candidate milliseconds) of the current batch."""
+        vt, ctas, cnt = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        self._check(self.lib.beamformer_gb300_batch_tuning(ctypes.byref(vt), ctypes.byref(ctas), None, 0,
+                                                           ctypes.byref(cnt)), "batch_tuning")
+        ms = np.zeros(max(cnt.value, 1), np.float32)
+        self._check(self.lib.beamformer_gb300_batch_tuning(None, None, ms.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                                           len(ms), ctypes.byref(cnt)), "batch_tuning")
+        return bool(vt.value), int(ctas.value), ms[:cnt.value]

@@ -1,0 +1,243 @@
+/*
+ * bf_das_hercules.cuh -- device code of the HERCULES delay-and-sum fast path
+ * (see bf_das_hercules.cu): the term, the per-voxel set-up and range proof, the
+ * column loop over receive channels and transmits, and one voxel tile.
+ */
+#pragma once
+#include "bf_kernels.h"
+#include "bf_das_math.cuh"
+
+namespace bf {
+
+/* Quotient x / b from the reciprocal rb = RN(1/b) and one correction FMA: equal
+ * to IEEE division wherever launch_verify_division found it so (for the DAS
+ * divisors: every |x| in [2^-100, 2^20]; x = 0 gives 0). */
+__device__ __forceinline__ float div_rc(float x, float b, float rb)
+{
+	const float q = __fmul_rn(x, rb);
+	const float r = fmaf(-q, b, x);
+	return fmaf(r, rb, q);
+}
+
+/* The part of one (voxel, transmit t, receive r) term after the lateral distance:
+ * lat2 = |lateral offset|^2 of the virtual element (r, t); row = (r * T + t) * S. */
+template <int INTERP, bool DEMOD, bool FASTMATH>
+__device__ __forceinline__ void term_tail(const DasParams &p, const float4 *__restrict__ tab, float lat2, float dz2,
+                                          float ka2, float dtx, float s_lim, int row, float scale, float &ax, float &ay)
+{
+	const float w    = ka2 * lat2;
+	const float x    = __fadd_rn(lat2, dz2);
+	const float drx  = FASTMATH ? sqrt_newton(x) : __fsqrt_rn(x);
+	const float d    = __fadd_rn(dtx, drx);
+	float tt = FASTMATH ? div_rc(d, p.c, p.rc) : __fdiv_rn(d, p.c);
+	tt = __fadd_rn(tt, p.toff);
+	const float idx = __fmul_rn(tt, p.fs);
+	const bool ok = idx >= 0.0f && idx < s_lim && w < HALF_PI_SQ;
+	const float a  = ok ? apod_cos2(w) * scale : 0.0f;
+	const float ic = ok ? idx : 1.0f;
+	float vx, vy;
+	if (INTERP == INTERP_NEAREST) {
+		const int j = row + (int)roundf(ic);
+		const int last = (int)p.rf_count - 1;
+		float2 v = __ldg(p.rf + min(j, last));
+		vx = j > last ? 0.0f : v.x;
+		vy = j > last ? 0.0f : v.y;
+	} else {
+		const int ii = (int)ic;
+		const float f = ic - (float)ii;
+		if (INTERP == INTERP_CUBIC) {
+			/* one 32-byte load of the segment (the table is 32-byte aligned) */
+			const float4 *cp = tab + 2 * (size_t)(unsigned)(row + ii);
+			float a0x, a0y, a1x, a1y, a2x, a2y, a3x, a3y;
+			asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+			    : "=f"(a0x), "=f"(a0y), "=f"(a1x), "=f"(a1y), "=f"(a2x), "=f"(a2y), "=f"(a3x), "=f"(a3y) : "l"(cp));
+			vx = fmaf(fmaf(fmaf(a3x, f, a2x), f, a1x), f, a0x);
+			vy = fmaf(fmaf(fmaf(a3y, f, a2y), f, a1y), f, a0y);
+		} else {
+			const float4 c = __ldg(tab + (size_t)(unsigned)(row + ii));
+			vx = fmaf(c.z, f, c.x);
+			vy = fmaf(c.w, f, c.y);
+		}
+	}
+	if (DEMOD) {
+		const float time = FASTMATH ? div_rc(ic, p.fs, p.rfs) : __fdiv_rn(ic, p.fs);
+		const float arg  = __fmul_rn(p.r360_fc, time);
+		const float k = rintf(arg * 0.159154943f);
+		float rr = fmaf(-k, 6.28125f, arg);
+		rr = fmaf(-k, 0x1.fb5444p-10f, rr);
+		float sn, cs;
+		__sincosf(rr, &sn, &cs);
+		const float ca = a * cs, sa = a * sn;
+		ax = fmaf(ca, vx, fmaf(-sa, vy, ax));
+		ay = fmaf(sa, vx, fmaf(ca, vy, ay));
+	} else {
+		ax = fmaf(a, vx, ax);
+		ay = fmaf(a, vy, ay);
+	}
+}
+
+/* Per-voxel constants of the term loop. */
+struct HercVoxel {
+	float q_fix, q_var;     /* lateral coordinates fixed by r and varied by t */
+	float dz2, dtx, ka2, lim2;
+	bool  fast;             /* every term inside the verified fast-math ranges */
+};
+
+__device__ __forceinline__ HercVoxel hercules_setup(const DasParams &p, int vx, int vy, int vz)
+{
+	HercVoxel v;
+	float w[3], q[3];
+	m4v(p.M, (float)vx, (float)vy, (float)vz, w);
+	m4v(p.X, w[0], w[1], w[2], q);
+	v.dz2 = __fmul_rn(q[2], q[2]);
+	v.dtx = transmit_distance(p, w, 0);
+	const float ka = __fdiv_rn(p.apod_scale, fabsf(q[2]));
+	v.ka2 = ka * ka;
+	v.lim2 = HALF_PI_SQ / v.ka2;
+	/* receive channel r fixes one lateral coordinate, transmit t the other */
+	v.q_fix = p.rx_cols ? q[0] : q[1];
+	v.q_var = p.rx_cols ? q[1] : q[0];
+	const float pitch_fix = p.rx_cols ? p.px : p.py, pitch_var = p.rx_cols ? p.py : p.px;
+	/* Bounds over all (r, t): the lateral offsets are linear in r and t, so their
+	 * largest magnitudes sit at the first or last element; the square-root argument
+	 * lies in [dz2, xmax] and |d| <= |dtx| + sqrt(xmax) (margins cover rounding). */
+	const float fa = fabsf(v.q_fix), fb = fabsf(v.q_fix - (float)(p.C - 1) * pitch_fix);
+	const float va = fabsf(v.q_var), vb = fabsf(v.q_var - (float)(p.T - 1) * pitch_var);
+	const float fm = fmaxf(fa, fb), vm = fmaxf(va, vb);
+	const float xmax = (fm * fm + vm * vm + v.dz2) * 1.0001f;
+	v.fast = p.fast_sqrt && v.dz2 >= p.sqrt_lo && xmax <= p.sqrt_hi &&
+	         fabsf(v.dtx) + sqrtf(xmax) * 1.0001f <= p.c_hi && p.c_lo <= 0x1p-100f &&
+	         p.fs_lo <= 0x1p-100f && (float)p.S <= p.fs_hi;
+	return v;
+}
+
+/* Sum over receive channels [u_begin, u_end) of the channel's transmit sum, for
+ * NV voxels that share their lateral coordinates (NV = 2: two depths of one
+ * column). The transmit interval is the widest of the voxels' (the deepest:
+ * the aperture grows with depth); a voxel's terms outside its own interval weigh
+ * exactly 0, so each voxel's sums equal its own loop's bit for bit. */
+template <int INTERP, bool DEMOD, bool FASTMATH, int NV>
+__device__ __forceinline__ void hercules_column(const DasParams &p, const float4 *__restrict__ tab, const HercVoxel *v,
+                                                int u_begin, int u_end, float *sx, float *sy)
+{
+	constexpr int extra = INTERP == INTERP_CUBIC ? 2 : INTERP == INTERP_LINEAR ? 1 : 0;
+	const float s_lim = (float)(p.S - extra);
+	const float pitch_fix = p.rx_cols ? p.px : p.py, pitch_var = p.rx_cols ? p.py : p.px;
+	const float q_fix = v[0].q_fix, q_var = v[0].q_var;
+	float lim2 = v[0].lim2;
+	#pragma unroll
+	for (int k = 1; k < NV; k++) lim2 = fmaxf(lim2, v[k].lim2);
+	for (int r = u_begin; r < u_end; r++) {
+		const float df = __fsub_rn(q_fix, __fmul_rn((float)r, pitch_fix));
+		const float f2 = __fmul_rn(df, df);
+		int t_lo, t_hi;
+		aperture_interval(q_var, pitch_var, lim2 - f2, p.T, t_lo, t_hi);
+		if (t_lo > t_hi) continue;
+		float ax[NV], ay[NV];
+		#pragma unroll
+		for (int k = 0; k < NV; k++) ax[k] = ay[k] = 0.0f;
+		int row = (r * p.T + t_lo) * p.S;
+		if (t_lo == 0) {
+			/* element 0 sits at 0: dv = q_var - 0 * pitch */
+			const float dv = __fsub_rn(q_var, __fmul_rn(0.0f, pitch_var));
+			const float lat2 = __fadd_rn(f2, __fmul_rn(dv, dv));
+			#pragma unroll
+			for (int k = 0; k < NV; k++)
+				term_tail<INTERP, DEMOD, FASTMATH>(p, tab, lat2, v[k].dz2, v[k].ka2, v[k].dtx, s_lim, row, p.inv_sqrt_T,
+				                                   ax[k], ay[k]);
+			t_lo = 1;
+			row += p.S;
+		}
+		float tf = (float)t_lo;
+		#pragma unroll (3 - NV)
+		for (int t = t_lo; t <= t_hi; t++) {
+			const float dv = __fsub_rn(q_var, __fmul_rn(tf, pitch_var));
+			const float lat2 = __fadd_rn(f2, __fmul_rn(dv, dv));
+			#pragma unroll
+			for (int k = 0; k < NV; k++)
+				term_tail<INTERP, DEMOD, FASTMATH>(p, tab, lat2, v[k].dz2, v[k].ka2, v[k].dtx, s_lim, row, 1.0f,
+				                                   ax[k], ay[k]);
+			tf += 1.0f;
+			row += p.S;
+		}
+		#pragma unroll
+		for (int k = 0; k < NV; k++) { sx[k] += ax[k]; sy[k] += ay[k]; }
+	}
+}
+
+/* One voxel on its own, with the fast or the IEEE square root and divisions. */
+template <int INTERP>
+__device__ __forceinline__ void hercules_single(const DasParams &p, const float4 *__restrict__ tab, const HercVoxel &v,
+                                             int u_begin, int u_end, float &sx, float &sy)
+{
+	const bool demod = p.fc > 0.0f;
+	if (v.fast) {
+		if (demod) hercules_column<INTERP, true, true, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else       hercules_column<INTERP, false, true, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+	} else {
+		if (demod) hercules_column<INTERP, true, false, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else       hercules_column<INTERP, false, false, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+	}
+}
+
+/* Voxel tiles of a block (128 threads). Volumes: threads 4 x 4 x 8, each thread
+ * two adjacent depths, so a block covers 4 x 4 x 16 voxels and a warp 4 x 4 x 4.
+ * Planes: threads 8 x 1 x 16, one voxel each. The sample delay moves by ~1.3
+ * samples per axial voxel step and by at most ~0.3 per lateral step inside the
+ * aperture, so the compact 3D warp reads the fewest distinct table entries per
+ * term; the spread of the transmit intervals across its lanes is ~3 elements. */
+template <int TY> struct HercTile {
+	static constexpr int X = TY == 1 ? 8 : 4, Y = TY, Z = 128 / (X * TY), NV = TY == 1 ? 1 : 2;
+};
+
+/* Thread threadIdx.x of voxel tile (bx, yt, bz), outer-loop group grp: the
+ * work of one das_hercules block, also run by the batched launch. */
+template <int INTERP, int TY>
+__device__ __forceinline__ void hercules_tile(const DasParams &p, const float4 *__restrict__ tab, int bx, int yt, int bz,
+                                              int grp)
+{
+	using Tile = HercTile<TY>;
+	constexpr int NV = Tile::NV;
+	const int vx = bx * Tile::X + (int)(threadIdx.x % Tile::X);
+	const int vy = yt * Tile::Y + (int)((threadIdx.x / Tile::X) % Tile::Y);
+	const int vz0 = (bz * Tile::Z + (int)(threadIdx.x / (Tile::X * Tile::Y))) * NV;
+	if (vx >= p.dims[0] || vy >= p.dims[1] || vz0 >= p.dims[2]) return;
+	const int u_begin = grp * p.per_group;
+	const int u_end   = min(p.loop_end, u_begin + p.per_group);
+
+	HercVoxel v[NV] = {};
+	float sx[NV], sy[NV];
+	int nv = 0;
+	#pragma unroll
+	for (int k = 0; k < NV; k++) {
+		sx[k] = sy[k] = 0.0f;
+		if (vz0 + k < p.dims[2]) { v[k] = hercules_setup(p, vx, vy, vz0 + k); nv = k + 1; }
+	}
+	bool together = nv == NV;
+	bool fast = v[0].fast;
+	#pragma unroll
+	for (int k = 1; k < NV; k++) {
+		together = together && v[k].q_fix == v[0].q_fix && v[k].q_var == v[0].q_var;
+		fast = fast && v[k].fast;
+	}
+	if (NV > 1 && together && fast) {
+		const bool demod = p.fc > 0.0f;
+		if (demod) hercules_column<INTERP, true, true, NV>(p, tab, v, u_begin, u_end, sx, sy);
+		else       hercules_column<INTERP, false, true, NV>(p, tab, v, u_begin, u_end, sx, sy);
+	} else {
+		#pragma unroll
+		for (int k = 0; k < NV; k++)
+			if (k < nv) hercules_single<INTERP>(p, tab, v[k], u_begin, u_end, sx[k], sy[k]);
+	}
+
+	const int64_t nvox = (int64_t)p.dims[0] * p.dims[1] * p.dims[2];
+	#pragma unroll
+	for (int k = 0; k < NV; k++) {
+		if (k >= nv) break;
+		const int64_t o = ((int64_t)(vz0 + k) * p.dims[1] + vy) * p.dims[0] + vx;
+		if (p.groups > 1) p.partial[grp * nvox + o] = make_float2(sx[k], sy[k]);
+		else              p.frame[o] = make_float2(sx[k], sy[k]);
+	}
+}
+
+} /* namespace bf */

@@ -131,6 +131,22 @@ cudaError_t launch_sum(float2 *out, const float2 *const *ins, int count, float p
                        cudaStream_t s);
 cudaError_t launch_min_max(const float2 *level0, const int32_t dims[3], int mips, float2 *levels, cudaStream_t s);
 
+/* Batched DAS (bf_das_batch.cu): many acquisitions' voxel tiles in one
+ * persistent launch. Each acquisition's DasParams has groups = 1. */
+enum DasBatchPath { DAS_BATCH_HERC_VOLUME = 0, DAS_BATCH_HERC_PLANE = 1, DAS_BATCH_GENERIC = 2 };
+struct DasBatchAcq {
+	DasParams     p;
+	const float4 *table;       /* HERCULES interpolation table (das_hercules_table_entries) */
+	int32_t       path;        /* DasBatchPath */
+	int32_t       reserved;
+};
+/* tile grid of an acquisition on a path; work items are int4 (acquisition, tile x, y, z) */
+void        das_batch_tiles(const DasParams &p, int path, int tiles[3]);
+cudaError_t launch_das_batch(const DasBatchAcq *acq, const int4 *items, int n_items, int *counter, int interp,
+                             int ctas, cudaStream_t s);
+/* the per-frame HERCULES interpolation table alone (cubic / linear; nothing for nearest) */
+cudaError_t launch_das_table(const DasParams &p, float4 *table, cudaStream_t s);
+
 /* DAS with its partial sums and tables in static device arrays (no allocation);
  * capacity in float2 partial-sum entries (groups x voxels) */
 cudaError_t launch_das_no_alloc(DasParams p, const float4 *focal4, const int16_t *sparse, cudaStream_t s);

@@ -234,6 +234,71 @@ bool ensure_frame(DeviceFrame &f, const int32_t dims[3])
 }
 
 /* (Re)build everything derived from the pushed state. */
+/* Channel mapping, sparse elements and focal vectors (sin/cos of the angle on
+ * the host) to the device. */
+bool upload_element_tables()
+{
+	float4 focal[256];
+	for (int i = 0; i < 256; i++) {
+		float angle = g.focal_vectors[2 * i] * DEG2RAD_F;
+		float depth = g.focal_vectors[2 * i + 1];
+		focal[i] = make_float4(sinf(angle), cosf(angle), depth, std::isinf(depth) ? 1.0f : 0.0f);
+	}
+	if (!cuda_ok(cudaMemcpy(g.d_chmap, g.channel_mapping, sizeof(g.channel_mapping), cudaMemcpyHostToDevice))) return false;
+	if (!cuda_ok(cudaMemcpy(g.d_sparse, g.sparse_elements, sizeof(g.sparse_elements), cudaMemcpyHostToDevice))) return false;
+	if (!cuda_ok(cudaMemcpy(g.d_focal, focal, sizeof(focal), cudaMemcpyHostToDevice))) return false;
+	return true;
+}
+
+/* Per-stage filter taps (polyphase arranged) and demodulation phasors of a plan. */
+bool build_stage_tables(const Plan &pl, StageTables *tables)
+{
+	for (int i = 0; i < pl.count; i++) {
+		int k = pl.shaders[i];
+		if (k != BeamformerShaderKind_Demodulate && k != BeamformerShaderKind_DemodulateFloat &&
+		    k != BeamformerShaderKind_Filter)
+			continue;
+		const bool is_filter = k == BeamformerShaderKind_Filter;
+		const std::vector<float> &h = g.taps[pl.slots[i] % BEAMFORMER_FILTER_SLOTS];
+		const uint32_t L = (uint32_t)h.size();
+		const uint32_t D = is_filter ? 1 : pl.demod_decimation;
+		const uint32_t Lp = (L + D - 1) / D, Lpad = Lp * D;
+		std::vector<float> hp((size_t)D * Lp, 0.0f);
+		for (uint32_t kp = Lpad - L; kp < Lpad; kp++) hp[(size_t)(kp % D) * Lp + kp / D] = h[Lpad - 1 - kp];
+		StageTables &st = tables[i];
+		if (hp.size() > st.taps_cap) {
+			cudaFree(st.taps);
+			st.taps = nullptr;
+			if (!cuda_ok(cudaMalloc(&st.taps, hp.size() * sizeof(float)))) return false;
+			st.taps_cap = hp.size();
+		}
+		if (!cuda_ok(cudaMemcpyAsync(st.taps, hp.data(), hp.size() * sizeof(float), cudaMemcpyHostToDevice, g.stream)))
+			return false;
+		cudaStreamSynchronize(g.stream);
+		if (!is_filter) {
+			const bool map = pl.demod_map != 0;
+			const uint32_t target = map ? pl.demod_st.out_channel / pl.demod_st.out_sample : pl.demod_st.out_transmit;
+			const uint32_t n_in = target * D;
+			std::vector<float2> ph(n_in);
+			const float r360 = 360.0f * DEG2RAD_F;
+			for (uint32_t j = 0; j < n_in; j++) {
+				/* filter.glsl rotate_iq(v, -j): radians(360) * f * index / fs */
+				float arg = r360 * pl.demod_frequency * (float)(-(int32_t)j) / pl.demod_fs;
+				ph[j] = make_float2(cosf(arg), sinf(arg));
+			}
+			if (n_in > st.phasor_cap) {
+				cudaFree(st.phasor);
+				st.phasor = nullptr;
+				if (!cuda_ok(cudaMalloc(&st.phasor, n_in * sizeof(float2)))) return false;
+				st.phasor_cap = n_in;
+			}
+			if (n_in && !cuda_ok(cudaMemcpy(st.phasor, ph.data(), n_in * sizeof(float2), cudaMemcpyHostToDevice)))
+				return false;
+		}
+	}
+	return true;
+}
+
 /* Precision variant: a first-stage int16 Hadamard Decode (fast Walsh-Hadamard
  * orders) writing fp16/bf16, followed by DemodulateFloat on the tensor cores, with
  * dense [channel][transmit][sample] layouts. Other pipelines fail UNSUPPORTED
@@ -337,61 +402,9 @@ bool prepare()
 	if (uses_decode && pl.decode_mode == DECODE_MODE_HADAMARD && !g.hadamard_ok)
 		return fail(BF_LIB_ERR_KIND_UNSUPPORTED), false;
 
-	/* per-stage filter taps (polyphase arranged) and demodulation phasors */
-	for (int i = 0; i < pl.count; i++) {
-		int k = pl.shaders[i];
-		if (k != BeamformerShaderKind_Demodulate && k != BeamformerShaderKind_DemodulateFloat &&
-		    k != BeamformerShaderKind_Filter)
-			continue;
-		const bool is_filter = k == BeamformerShaderKind_Filter;
-		const std::vector<float> &h = g.taps[pl.slots[i] % BEAMFORMER_FILTER_SLOTS];
-		const uint32_t L = (uint32_t)h.size();
-		const uint32_t D = is_filter ? 1 : pl.demod_decimation;
-		const uint32_t Lp = (L + D - 1) / D, Lpad = Lp * D;
-		std::vector<float> hp((size_t)D * Lp, 0.0f);
-		for (uint32_t kp = Lpad - L; kp < Lpad; kp++) hp[(size_t)(kp % D) * Lp + kp / D] = h[Lpad - 1 - kp];
-		StageTables &st = g.stage_tables[i];
-		if (hp.size() > st.taps_cap) {
-			cudaFree(st.taps);
-			st.taps = nullptr;
-			if (!cuda_ok(cudaMalloc(&st.taps, hp.size() * sizeof(float)))) return false;
-			st.taps_cap = hp.size();
-		}
-		if (!cuda_ok(cudaMemcpyAsync(st.taps, hp.data(), hp.size() * sizeof(float), cudaMemcpyHostToDevice, g.stream)))
-			return false;
-		cudaStreamSynchronize(g.stream);
-		if (!is_filter) {
-			const bool map = pl.demod_map != 0;
-			const uint32_t target = map ? pl.demod_st.out_channel / pl.demod_st.out_sample : pl.demod_st.out_transmit;
-			const uint32_t n_in = target * D;
-			std::vector<float2> ph(n_in);
-			const float r360 = 360.0f * DEG2RAD_F;
-			for (uint32_t j = 0; j < n_in; j++) {
-				/* filter.glsl rotate_iq(v, -j): radians(360) * f * index / fs */
-				float arg = r360 * pl.demod_frequency * (float)(-(int32_t)j) / pl.demod_fs;
-				ph[j] = make_float2(cosf(arg), sinf(arg));
-			}
-			if (n_in > st.phasor_cap) {
-				cudaFree(st.phasor);
-				st.phasor = nullptr;
-				if (!cuda_ok(cudaMalloc(&st.phasor, n_in * sizeof(float2)))) return false;
-				st.phasor_cap = n_in;
-			}
-			if (n_in && !cuda_ok(cudaMemcpy(st.phasor, ph.data(), n_in * sizeof(float2), cudaMemcpyHostToDevice)))
-				return false;
-		}
-	}
+	if (!build_stage_tables(pl, g.stage_tables)) return false;
 
-	/* channel mapping, sparse elements, focal vectors (sin/cos of the angle on the host) */
-	float4 focal[256];
-	for (int i = 0; i < 256; i++) {
-		float angle = g.focal_vectors[2 * i] * DEG2RAD_F;
-		float depth = g.focal_vectors[2 * i + 1];
-		focal[i] = make_float4(sinf(angle), cosf(angle), depth, std::isinf(depth) ? 1.0f : 0.0f);
-	}
-	if (!cuda_ok(cudaMemcpy(g.d_chmap, g.channel_mapping, sizeof(g.channel_mapping), cudaMemcpyHostToDevice))) return false;
-	if (!cuda_ok(cudaMemcpy(g.d_sparse, g.sparse_elements, sizeof(g.sparse_elements), cudaMemcpyHostToDevice))) return false;
-	if (!cuda_ok(cudaMemcpy(g.d_focal, focal, sizeof(focal), cudaMemcpyHostToDevice))) return false;
+	if (!upload_element_tables()) return false;
 
 	voxel_transform(pl.das, g.M);
 	g.plan_ok = true;
@@ -511,6 +524,148 @@ void collect_timings(bool block)
 	}
 }
 
+/* Decode stage i of a plan: src = the pushed RF (first stage), in_buf / out_buf =
+ * channel buffers of buf_bytes each. */
+void fill_decode_params(const Plan &pl, int i, const void *src, uint64_t src_bytes, void *in_buf, void *out_buf,
+                        uint64_t buf_bytes, const int8_t *hadamard, int sylvester, int base, DecodeParams &p)
+{
+	const int kind = pl.shaders[i];
+	const bool first = i == 0;
+	p.first_stage = first;
+	if (first) {
+		p.in = src;
+		switch (g.data_kind) {
+		case BeamformerDataKind_Int16Complex:   p.input = DEC_IN_I16C; p.in_elems = src_bytes / 4; break;
+		case BeamformerDataKind_Float32:        p.input = DEC_IN_F32;  p.in_elems = src_bytes / 4; break;
+		case BeamformerDataKind_Float32Complex: p.input = DEC_IN_F32C; p.in_elems = src_bytes / 8; break;
+		default:                                p.input = DEC_IN_I16;  p.in_elems = src_bytes / 2; break;
+		}
+		p.channel_map = g.d_chmap;
+	} else {
+		p.in = in_buf;
+		p.input = kind == BeamformerShaderKind_DecodeInt16Complex ? DEC_IN_I16C : DEC_IN_F32C;
+		p.in_elems = buf_bytes / (p.input == DEC_IN_I16C ? 4 : 8);
+		p.channel_map = nullptr;
+	}
+	p.out = (float *)out_buf;
+	p.out_vec2 = buf_bytes / 8;
+	p.hadamard = hadamard;
+	p.st = pl.decode_st;
+	p.output = kind == BeamformerShaderKind_DecodeInt16ToFloat ? DEC_OUT_REAL_PAIRS : DEC_OUT_COMPLEX;
+	/* samples the reference's dispatch writes: pass-2 guard (time sample < output
+	 * transmit stride) and grid width; int16 data decoded first packs two samples
+	 * per invocation */
+	const uint32_t ots = pl.decode_st.out_transmit, cov = pl.decode_invocations_x;
+	const bool pairs = first && g.data_kind == BeamformerDataKind_Int16;
+	if (p.output == DEC_OUT_REAL_PAIRS || p.output == DEC_OUT_REAL_F16 || p.output == DEC_OUT_REAL_BF16)
+		p.samples = 2 * std::min(ots, cov);
+	else if (pairs)
+		p.samples = 2 * std::min((ots + 1) / 2, cov);
+	else
+		p.samples = std::min(ots, cov);
+	/* pass-1 gather guard: time sample < input transmit stride */
+	p.in_limit = first ? (pairs ? (pl.decode_st.in_transmit + 1) / 2 * 2 : pl.decode_st.in_transmit) : 0xFFFFFFFFu;
+	p.channels = pl.das.dec_data_dim[1];
+	p.transmits = pl.transmit_count;
+	p.sylvester = (uint32_t)sylvester;
+	p.base = (uint32_t)base;
+	p.hadamard_mode = pl.decode_mode == DECODE_MODE_HADAMARD;
+}
+
+/* Demodulate / Filter stage i of a plan (see fill_decode_params). */
+void fill_filter_params(const Plan &pl, int i, const void *src, uint64_t src_bytes, void *in_buf, void *out_buf,
+                        uint64_t buf_bytes, const StageTables &st, FilterParams &p)
+{
+	const int kind = pl.shaders[i];
+	const bool is_filter = kind == BeamformerShaderKind_Filter;
+	const bool map = !is_filter && pl.demod_map;
+	p.kind = is_filter ? FILT_COMPLEX : kind == BeamformerShaderKind_Demodulate ? FILT_DEMOD_I16 : FILT_DEMOD_F32;
+	if (map) {
+		p.in = src;
+		p.in_elems = src_bytes / (p.kind == FILT_DEMOD_I16 ? 4 : 8);
+	} else {
+		p.in = in_buf;
+		p.in_elems = buf_bytes / 8;
+	}
+	p.out = out_buf;
+	p.out_elems = buf_bytes / (p.kind == FILT_DEMOD_I16 ? 4 : 8);
+	p.st = is_filter ? pl.filter_st : pl.demod_st;
+	p.decimation = is_filter ? 1 : pl.demod_decimation;
+	p.map_channels = map;
+	p.channel_map = g.d_chmap;
+	p.out_samples = map ? p.st.out_channel / p.st.out_sample : p.st.out_transmit;
+	p.in_samples = p.out_samples * p.decimation;
+	p.channels = pl.das.dec_data_dim[1];
+	p.transmits = pl.das.dec_data_dim[2];
+	p.taps = st.taps;
+	p.phasor = st.phasor;
+	p.taps_len = (uint32_t)g.taps[pl.slots[i] % BEAMFORMER_FILTER_SLOTS].size();
+}
+
+/* DAS stage of a plan reading channel data rf (rf_bytes readable) into frame
+ * (dims, voxel transform M); the outer loop is not split (groups = 1). */
+bool fill_das_params(const Plan &pl, int kind, const void *rf, uint64_t rf_bytes, float2 *frame,
+                     const int32_t dims[3], const float M[16], DasParams &p)
+{
+	const BeamformerParameters &d = pl.das;
+	p.rf = (const float2 *)rf;
+	uint64_t readable = pl.rf_size / 8;
+	p.rf_count = (int64_t)(readable < rf_bytes / 8 ? readable : rf_bytes / 8);
+	p.frame = frame;
+	std::memcpy(p.dims, dims, sizeof(p.dims));
+	std::memcpy(p.M, M, sizeof(p.M));
+	std::memcpy(p.X, d.xdc_transform, sizeof(p.X));
+	p.S = (int32_t)d.dec_data_dim[0];
+	p.C = (int32_t)d.dec_data_dim[1];
+	p.T = (int32_t)d.dec_data_dim[2];
+	p.das_id = (int32_t)d.das_shader_id;
+	switch (d.das_shader_id) {
+	case DASShaderKind_FORCES: case DASShaderKind_UFORCES:       p.family = DAS_FORCES; break;
+	case DASShaderKind_HERCULES: case DASShaderKind_UHERCULES:   p.family = DAS_HERCULES; break;
+	case DASShaderKind_RCA_VLS: case DASShaderKind_RCA_TPW:
+	case DASShaderKind_FLASH:                                     p.family = DAS_RCA; break;
+	default:                                                      p.family = DAS_NONE; break;
+	}
+	p.sparse_mode = d.das_shader_id == DASShaderKind_UFORCES || d.das_shader_id == DASShaderKind_UHERCULES;
+	p.fast = kind == BeamformerShaderKind_DASFast;
+	p.coherency = d.coherency_weighting != 0;
+	p.interp = g.interpolation_override >= 0 ? g.interpolation_override : (d.interpolate ? INTERP_CUBIC : INTERP_NEAREST);
+	p.tx_rows = !((d.transmit_mode & 2) != 0);
+	p.rx_cols = (d.transmit_mode & 1) != 0;
+	p.rx_rows = !p.rx_cols;
+	p.loop_end = (d.das_shader_id == DASShaderKind_RCA_VLS || d.das_shader_id == DASShaderKind_RCA_TPW) ? p.T : p.C;
+	p.fs = d.sampling_frequency;
+	p.fc = d.center_frequency;
+	p.c = d.speed_of_sound;
+	p.toff = d.time_offset;
+	const float r360 = 360.0f * DEG2RAD_F;
+	p.r360_fc = r360 * d.center_frequency;
+	p.apod_scale = d.f_number * (180.0f * DEG2RAD_F);
+	p.apod_hi = 0.25f * r360;
+	p.inv_sqrt_T = 1.0f / sqrtf((float)p.T);
+	p.px = d.xdc_element_pitch[0];
+	p.py = d.xdc_element_pitch[1];
+	p.cy_forces = p.py * (float)(p.C / 2);
+	p.focal = g.d_focal;
+	p.sparse = g.d_sparse;
+	p.rc = 1.0f / p.c;
+	p.rfs = 1.0f / p.fs;
+	/* distances and sample indices in [2^-100, 2^20] (below, the quotients by
+	 * c and fs would be subnormal) */
+	if (!division_range(p.c, 0x1p-100f, 0x1p20f, p.c_lo, p.c_hi)) return false;
+	if (!division_range(p.fs, 0x1p-100f, 0x1p20f, p.fs_lo, p.fs_hi)) return false;
+	p.fast_sqrt = sqrt_verified() ? 1 : 0;
+	p.sqrt_lo = 0x1p-100f;
+	p.sqrt_hi = 0x1p30f;
+	{
+		const int64_t dense = (int64_t)p.C * p.T * p.S;
+		p.dense_rows = p.rf_count >= dense && dense < (1ll << 31) && p.S >= 4;
+	}
+	p.groups = 1;
+	p.per_group = p.loop_end;
+	return true;
+}
+
 bool run_stage(int i, const void *src, uint64_t src_bytes, DeviceFrame &frame, bool &did_sum, int &sum_target)
 {
 	const Plan &pl = g.plan;
@@ -528,47 +683,12 @@ bool run_stage(int i, const void *src, uint64_t src_bytes, DeviceFrame &frame, b
 	case BeamformerShaderKind_DecodeFloatComplex:
 	case BeamformerShaderKind_DecodeInt16ToFloat: {
 		DecodeParams p{};
-		const bool first = i == 0;
-		p.first_stage = first;
-		if (first) {
-			p.in = src;
-			switch (g.data_kind) {
-			case BeamformerDataKind_Int16Complex:   p.input = DEC_IN_I16C; p.in_elems = src_bytes / 4; break;
-			case BeamformerDataKind_Float32:        p.input = DEC_IN_F32;  p.in_elems = src_bytes / 4; break;
-			case BeamformerDataKind_Float32Complex: p.input = DEC_IN_F32C; p.in_elems = src_bytes / 8; break;
-			default:                                p.input = DEC_IN_I16;  p.in_elems = src_bytes / 2; break;
-			}
-			p.channel_map = g.d_chmap;
-		} else {
-			p.in = g.chan[in_idx];
-			p.input = kind == BeamformerShaderKind_DecodeInt16Complex ? DEC_IN_I16C : DEC_IN_F32C;
-			p.in_elems = g.chan_bytes / (p.input == DEC_IN_I16C ? 4 : 8);
-			p.channel_map = nullptr;
+		fill_decode_params(pl, i, src, src_bytes, g.chan[in_idx], g.chan[out_idx], g.chan_bytes, g.hadamard,
+		                   g.hadamard_sylvester, g.hadamard_base, p);
+		if (g.tc_active && i == 0) {
+			p.output = g.precision == 2 ? DEC_OUT_REAL_BF16 : DEC_OUT_REAL_F16;
+			p.samples = 2 * std::min(pl.decode_st.out_transmit, pl.decode_invocations_x);
 		}
-		p.out = (float *)g.chan[out_idx];
-		p.out_vec2 = g.chan_bytes / 8;
-		p.hadamard = g.hadamard;
-		p.st = pl.decode_st;
-		p.output = kind == BeamformerShaderKind_DecodeInt16ToFloat ? DEC_OUT_REAL_PAIRS : DEC_OUT_COMPLEX;
-		if (g.tc_active && i == 0) p.output = g.precision == 2 ? DEC_OUT_REAL_BF16 : DEC_OUT_REAL_F16;
-		/* samples the reference's dispatch writes: pass-2 guard (time sample < output
-		 * transmit stride) and grid width; int16 data decoded first packs two samples
-		 * per invocation */
-		const uint32_t ots = pl.decode_st.out_transmit, cov = pl.decode_invocations_x;
-		const bool pairs = first && g.data_kind == BeamformerDataKind_Int16;
-		if (p.output == DEC_OUT_REAL_PAIRS || p.output == DEC_OUT_REAL_F16 || p.output == DEC_OUT_REAL_BF16)
-			p.samples = 2 * std::min(ots, cov);
-		else if (pairs)
-			p.samples = 2 * std::min((ots + 1) / 2, cov);
-		else
-			p.samples = std::min(ots, cov);
-		/* pass-1 gather guard: time sample < input transmit stride */
-		p.in_limit = first ? (pairs ? (pl.decode_st.in_transmit + 1) / 2 * 2 : pl.decode_st.in_transmit) : 0xFFFFFFFFu;
-		p.channels = bp.dec_data_dim[1];
-		p.transmits = pl.transmit_count;
-		p.sylvester = (uint32_t)g.hadamard_sylvester;
-		p.base = (uint32_t)g.hadamard_base;
-		p.hadamard_mode = pl.decode_mode == DECODE_MODE_HADAMARD;
 		err = launch_decode(p, g.stream);
 		g.last_chan = out_idx;
 	} break;
@@ -587,89 +707,14 @@ bool run_stage(int i, const void *src, uint64_t src_bytes, DeviceFrame &frame, b
 			break;
 		}
 		FilterParams p{};
-		const bool is_filter = kind == BeamformerShaderKind_Filter;
-		const bool map = !is_filter && pl.demod_map;
-		p.kind = is_filter ? FILT_COMPLEX : kind == BeamformerShaderKind_Demodulate ? FILT_DEMOD_I16 : FILT_DEMOD_F32;
-		if (map) {
-			p.in = src;
-			p.in_elems = src_bytes / (p.kind == FILT_DEMOD_I16 ? 4 : 8);
-		} else {
-			p.in = g.chan[in_idx];
-			p.in_elems = g.chan_bytes / 8;
-		}
-		p.out = g.chan[out_idx];
-		p.out_elems = g.chan_bytes / (p.kind == FILT_DEMOD_I16 ? 4 : 8);
-		p.st = is_filter ? pl.filter_st : pl.demod_st;
-		p.decimation = is_filter ? 1 : pl.demod_decimation;
-		p.map_channels = map;
-		p.channel_map = g.d_chmap;
-		p.out_samples = map ? p.st.out_channel / p.st.out_sample : p.st.out_transmit;
-		p.in_samples = p.out_samples * p.decimation;
-		p.channels = pl.das.dec_data_dim[1];
-		p.transmits = pl.das.dec_data_dim[2];
-		p.taps = g.stage_tables[i].taps;
-		p.phasor = g.stage_tables[i].phasor;
-		p.taps_len = (uint32_t)g.taps[pl.slots[i] % BEAMFORMER_FILTER_SLOTS].size();
+		fill_filter_params(pl, i, src, src_bytes, g.chan[in_idx], g.chan[out_idx], g.chan_bytes, g.stage_tables[i], p);
 		err = launch_filter(p, g.stream);
 		g.last_chan = out_idx;
 	} break;
 	case BeamformerShaderKind_DAS:
 	case BeamformerShaderKind_DASFast: {
-		const BeamformerParameters &d = pl.das;
 		DasParams p{};
-		p.rf = g.chan[in_idx];
-		uint64_t readable = pl.rf_size / 8;
-		p.rf_count = (int64_t)(readable < g.chan_bytes / 8 ? readable : g.chan_bytes / 8);
-		p.frame = frame.data;
-		std::memcpy(p.dims, frame.dims, sizeof(p.dims));
-		std::memcpy(p.M, g.M, sizeof(p.M));
-		std::memcpy(p.X, d.xdc_transform, sizeof(p.X));
-		p.S = (int32_t)d.dec_data_dim[0];
-		p.C = (int32_t)d.dec_data_dim[1];
-		p.T = (int32_t)d.dec_data_dim[2];
-		p.das_id = (int32_t)d.das_shader_id;
-		switch (d.das_shader_id) {
-		case DASShaderKind_FORCES: case DASShaderKind_UFORCES:       p.family = DAS_FORCES; break;
-		case DASShaderKind_HERCULES: case DASShaderKind_UHERCULES:   p.family = DAS_HERCULES; break;
-		case DASShaderKind_RCA_VLS: case DASShaderKind_RCA_TPW:
-		case DASShaderKind_FLASH:                                     p.family = DAS_RCA; break;
-		default:                                                      p.family = DAS_NONE; break;
-		}
-		p.sparse_mode = d.das_shader_id == DASShaderKind_UFORCES || d.das_shader_id == DASShaderKind_UHERCULES;
-		p.fast = kind == BeamformerShaderKind_DASFast;
-		p.coherency = d.coherency_weighting != 0;
-		p.interp = g.interpolation_override >= 0 ? g.interpolation_override : (d.interpolate ? INTERP_CUBIC : INTERP_NEAREST);
-		p.tx_rows = !((d.transmit_mode & 2) != 0);
-		p.rx_cols = (d.transmit_mode & 1) != 0;
-		p.rx_rows = !p.rx_cols;
-		p.loop_end = (d.das_shader_id == DASShaderKind_RCA_VLS || d.das_shader_id == DASShaderKind_RCA_TPW) ? p.T : p.C;
-		p.fs = d.sampling_frequency;
-		p.fc = d.center_frequency;
-		p.c = d.speed_of_sound;
-		p.toff = d.time_offset;
-		const float r360 = 360.0f * DEG2RAD_F;
-		p.r360_fc = r360 * d.center_frequency;
-		p.apod_scale = d.f_number * (180.0f * DEG2RAD_F);
-		p.apod_hi = 0.25f * r360;
-		p.inv_sqrt_T = 1.0f / sqrtf((float)p.T);
-		p.px = d.xdc_element_pitch[0];
-		p.py = d.xdc_element_pitch[1];
-		p.cy_forces = p.py * (float)(p.C / 2);
-		p.focal = g.d_focal;
-		p.sparse = g.d_sparse;
-		p.rc = 1.0f / p.c;
-		p.rfs = 1.0f / p.fs;
-		/* distances and sample indices in [2^-100, 2^20] (below, the quotients by
-		 * c and fs would be subnormal) */
-		if (!division_range(p.c, 0x1p-100f, 0x1p20f, p.c_lo, p.c_hi)) return false;
-		if (!division_range(p.fs, 0x1p-100f, 0x1p20f, p.fs_lo, p.fs_hi)) return false;
-		p.fast_sqrt = sqrt_verified() ? 1 : 0;
-		p.sqrt_lo = 0x1p-100f;
-		p.sqrt_hi = 0x1p30f;
-		{
-			const int64_t dense = (int64_t)p.C * p.T * p.S;
-			p.dense_rows = p.rf_count >= dense && dense < (1ll << 31) && p.S >= 4;
-		}
+		if (!fill_das_params(pl, kind, g.chan[in_idx], g.chan_bytes, frame.data, frame.dims, g.M, p)) return false;
 		/* small volumes: split the outer loop over block groups so the grid fills the GPU */
 		p.groups = 1;
 		p.per_group = p.loop_end;
@@ -843,6 +888,277 @@ const char *error_text(int32_t kind)
 	const int32_t n = (int32_t)(sizeof(table) / sizeof(table[0]));
 	if (kind < 0 || kind >= n - 1) return table[n - 1];
 	return table[kind];
+}
+
+
+/* ------------------------------ batched beamforming ----------------------------- */
+
+/* One acquisition of a batch: its plan, channel buffers and tables. */
+struct BatchAcqState {
+	Plan        plan{};
+	void       *chan[2] = {nullptr, nullptr};
+	uint64_t    chan_bytes = 0;
+	StageTables tables[MAX_COMPUTE_SHADER_STAGES];
+	float4     *das_table = nullptr;
+	int8_t     *hadamard = nullptr;
+	int32_t     sylvester = 0, base = 0;
+	float       M[16] = {};
+	DasParams   das{};
+	int32_t     path = DAS_BATCH_GENERIC;
+	const void *rf = nullptr;
+	uint64_t    rf_bytes = 0;
+};
+
+struct BatchState {
+	uint64_t                   signature = 0;
+	std::vector<BatchAcqState> acq;
+	DasBatchAcq               *d_acq = nullptr;
+	int4                      *d_items = nullptr;
+	size_t                     items_cap = 0;
+	int                       *d_counter = nullptr;
+	int                        n_items = 0;
+	int                        interp = INTERP_NEAREST;
+	int                        ctas = 0;
+	bool                       volume_tiles = true;
+	cudaGraphExec_t            exec = nullptr;
+	uint64_t                   graph_kernels = 0;
+	std::vector<float>         candidate_ms;          /* autotuner: (tiles, ctas) candidates in order */
+};
+BatchState gb;
+
+void free_batch()
+{
+	if (g.ready) cudaStreamSynchronize(g.stream);
+	if (gb.exec) cudaGraphExecDestroy(gb.exec);
+	for (auto &a : gb.acq) {
+		cudaFree(a.chan[0]);
+		cudaFree(a.chan[1]);
+		for (auto &t : a.tables) { cudaFree(t.taps); cudaFree(t.phasor); }
+		cudaFree(a.das_table);
+		cudaFree(a.hadamard);
+	}
+	cudaFree(gb.d_acq);
+	cudaFree(gb.d_items);
+	cudaFree(gb.d_counter);
+	gb = BatchState();
+}
+
+uint64_t fnv1a(uint64_t h, const void *data, size_t n)
+{
+	const uint8_t *b = (const uint8_t *)data;
+	for (size_t i = 0; i < n; i++) h = (h ^ b[i]) * 1099511628211ull;
+	return h;
+}
+
+uint64_t batch_signature(const BeamformerParameters *params, uint32_t count, const void *const *rf,
+                         const uint64_t *rf_size, float *const *out)
+{
+	uint64_t h = 1469598103934665603ull;
+	h = fnv1a(h, &count, sizeof(count));
+	h = fnv1a(h, params, sizeof(BeamformerParameters) * count);
+	h = fnv1a(h, rf, sizeof(void *) * count);
+	h = fnv1a(h, rf_size, sizeof(uint64_t) * count);
+	h = fnv1a(h, out, sizeof(float *) * count);
+	h = fnv1a(h, g.shaders, sizeof(g.shaders));
+	h = fnv1a(h, g.slots, sizeof(g.slots));
+	h = fnv1a(h, &g.shader_count, sizeof(g.shader_count));
+	h = fnv1a(h, &g.data_kind, sizeof(g.data_kind));
+	for (int i = 0; i < BEAMFORMER_FILTER_SLOTS; i++) h = fnv1a(h, g.taps[i].data(), g.taps[i].size() * sizeof(float));
+	h = fnv1a(h, g.channel_mapping, sizeof(g.channel_mapping));
+	h = fnv1a(h, g.sparse_elements, sizeof(g.sparse_elements));
+	h = fnv1a(h, g.focal_vectors, sizeof(g.focal_vectors));
+	h = fnv1a(h, &g.interpolation_override, sizeof(g.interpolation_override));
+	return h;
+}
+
+/* Front end (decode / demodulate / filter stages) of every acquisition, the
+ * HERCULES interpolation tables, then the one persistent DAS launch. */
+cudaError_t batch_launch(cudaStream_t s)
+{
+	for (auto &a : gb.acq) {
+		const Plan &pl = a.plan;
+		int last = -1;
+		for (int i = 0; i + 1 < pl.count; i++) {
+			const int kind = pl.shaders[i];
+			const int out_idx = last < 0 ? 0 : 1 - last, in_idx = last < 0 ? 0 : last;
+			cudaError_t e = cudaSuccess;
+			if (kind == BeamformerShaderKind_Demodulate || kind == BeamformerShaderKind_DemodulateFloat ||
+			    kind == BeamformerShaderKind_Filter) {
+				FilterParams p{};
+				fill_filter_params(pl, i, a.rf, a.rf_bytes, a.chan[in_idx], a.chan[out_idx], a.chan_bytes, a.tables[i], p);
+				e = launch_filter(p, s);
+			} else {
+				DecodeParams p{};
+				fill_decode_params(pl, i, a.rf, a.rf_bytes, a.chan[in_idx], a.chan[out_idx], a.chan_bytes, a.hadamard,
+				                   a.sylvester, a.base, p);
+				e = launch_decode(p, s);
+			}
+			if (e != cudaSuccess) return e;
+			last = out_idx;
+		}
+		if (a.path != DAS_BATCH_GENERIC && a.das.interp != INTERP_NEAREST) {
+			const cudaError_t e = launch_das_table(a.das, a.das_table, s);
+			if (e != cudaSuccess) return e;
+		}
+	}
+	return launch_das_batch(gb.d_acq, gb.d_items, gb.n_items, gb.d_counter, gb.interp, gb.ctas, s);
+}
+
+/* Paths and the cost-ordered work list for a tile choice; uploads both. */
+bool batch_items(bool volume_tiles)
+{
+	std::vector<DasBatchAcq> acqs(gb.acq.size());
+	struct Entry { double cost; int acq; };
+	std::vector<Entry> order;
+	for (size_t i = 0; i < gb.acq.size(); i++) {
+		BatchAcqState &a = gb.acq[i];
+		if (a.das.family == DAS_HERCULES)
+			a.path = volume_tiles && a.das.dims[1] >= 4 ? DAS_BATCH_HERC_VOLUME : DAS_BATCH_HERC_PLANE;
+		acqs[i].p = a.das;
+		acqs[i].table = a.das_table;
+		acqs[i].path = a.path;
+		const double vox = a.path == DAS_BATCH_HERC_VOLUME ? 256.0 : 128.0;
+		order.push_back({vox * a.das.T * a.das.C, (int)i});
+	}
+	std::stable_sort(order.begin(), order.end(), [](const Entry &x, const Entry &y) { return x.cost > y.cost; });
+	std::vector<int4> items;
+	for (const Entry &e : order) {
+		int tiles[3];
+		das_batch_tiles(gb.acq[e.acq].das, gb.acq[e.acq].path, tiles);
+		for (int z = 0; z < tiles[2]; z++)
+			for (int y = 0; y < tiles[1]; y++)
+				for (int x = 0; x < tiles[0]; x++) items.push_back(make_int4(e.acq, x, y, z));
+	}
+	if (items.size() > gb.items_cap) {
+		cudaFree(gb.d_items);
+		gb.d_items = nullptr;
+		if (!cuda_ok(cudaMalloc(&gb.d_items, items.size() * sizeof(int4)))) return false;
+		gb.items_cap = items.size();
+	}
+	gb.n_items = (int)items.size();
+	if (!cuda_ok(cudaMemcpy(gb.d_items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice))) return false;
+	return cuda_ok(cudaMemcpy(gb.d_acq, acqs.data(), acqs.size() * sizeof(DasBatchAcq), cudaMemcpyHostToDevice));
+}
+
+/* Plans, buffers and tables of a new batch; autotunes the DAS launch (tile
+ * shape of HERCULES volumes x CTAs per SM, timed on the device) and captures
+ * the whole batch in a CUDA graph. */
+bool build_batch(const BeamformerParameters *params, uint32_t count, const void *const *rf, const uint64_t *rf_size,
+                 float *const *out)
+{
+	free_batch();
+	if (!upload_element_tables()) return false;
+	gb.acq.resize(count);
+	int interp = -1;
+	bool any_volume = false;
+	for (uint32_t i = 0; i < count; i++) {
+		BatchAcqState &a = gb.acq[i];
+		plan_pipeline(params[i], g.shaders, g.slots, g.shader_count, g.data_kind, g.filters, a.plan);
+		const Plan &pl = a.plan;
+		if (pl.count < 1 || pl.shaders[pl.count - 1] != BeamformerShaderKind_DASFast) return fail(BF_LIB_ERR_KIND_UNSUPPORTED), false;
+		for (int s = 0; s + 1 < pl.count; s++) {
+			const int k = pl.shaders[s];
+			const bool ok = k == BeamformerShaderKind_Decode || k == BeamformerShaderKind_DecodeInt16ToFloat ||
+			                k == BeamformerShaderKind_DecodeInt16Complex || k == BeamformerShaderKind_DecodeFloat ||
+			                k == BeamformerShaderKind_DecodeFloatComplex || k == BeamformerShaderKind_CudaDecode ||
+			                k == BeamformerShaderKind_Demodulate || k == BeamformerShaderKind_DemodulateFloat ||
+			                k == BeamformerShaderKind_Filter;
+			if (!ok) return fail(BF_LIB_ERR_KIND_UNSUPPORTED), false;
+			if (k == BeamformerShaderKind_Demodulate || k == BeamformerShaderKind_DemodulateFloat || k == BeamformerShaderKind_Filter) {
+				const FilterSpec &f = g.filters[pl.slots[s] % BEAMFORMER_FILTER_SLOTS];
+				if (f.kind < 0 || f.length <= 0) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS), false;
+			}
+		}
+		a.rf = rf[i];
+		a.rf_bytes = rf_size[i];
+		a.chan_bytes = 8ull * params[i].dec_data_dim[0] * params[i].dec_data_dim[1] * params[i].dec_data_dim[2];
+		for (int b = 0; b < 2; b++) {
+			if (!cuda_ok(cudaMalloc(&a.chan[b], a.chan_bytes))) return false;
+			if (!cuda_ok(cudaMemset(a.chan[b], 0, a.chan_bytes))) return false;
+		}
+		if (pl.decode_mode == DECODE_MODE_HADAMARD) {
+			std::vector<int8_t> h;
+			if (!hadamard_matrix((int32_t)params[i].dec_data_dim[2], h, a.sylvester, a.base))
+				return fail(BF_LIB_ERR_KIND_UNSUPPORTED), false;
+			if (!cuda_ok(cudaMalloc(&a.hadamard, h.size()))) return false;
+			if (!cuda_ok(cudaMemcpy(a.hadamard, h.data(), h.size(), cudaMemcpyHostToDevice))) return false;
+		}
+		if (!build_stage_tables(pl, a.tables)) return false;
+		voxel_transform(pl.das, a.M);
+		int last = -1;
+		for (int s = 0; s + 1 < pl.count; s++) last = last < 0 ? 0 : 1 - last;
+		int32_t dims[3];
+		for (int k = 0; k < 3; k++) dims[k] = pl.das.output_points[k] > 1 ? pl.das.output_points[k] : 1;
+		if (!fill_das_params(pl, BeamformerShaderKind_DASFast, a.chan[last < 0 ? 0 : last], a.chan_bytes,
+		                     (float2 *)out[i], dims, a.M, a.das))
+			return false;
+		if (last < 0) { a.das.rf = (const float2 *)rf[i]; a.das.rf_count = (int64_t)(std::min<uint64_t>(pl.rf_size, rf_size[i]) / 8); }
+		if (a.das.family == DAS_HERCULES && das_hercules_supported(a.das)) {
+			a.path = DAS_BATCH_HERC_PLANE;
+			any_volume = any_volume || a.das.dims[1] >= 4;
+			const uint64_t n = (uint64_t)das_hercules_table_entries(a.das);
+			if (n && !cuda_ok(cudaMalloc(&a.das_table, n * sizeof(float4)))) return false;
+		} else if (a.das.family == DAS_FORCES && !a.das.sparse_mode) {
+			a.path = DAS_BATCH_GENERIC;
+		} else {
+			return fail(BF_LIB_ERR_KIND_UNSUPPORTED), false;
+		}
+		if (interp >= 0 && a.das.interp != interp) return fail(BF_LIB_ERR_KIND_UNSUPPORTED), false;
+		interp = a.das.interp;
+	}
+	gb.interp = interp;
+	if (!cuda_ok(cudaMalloc(&gb.d_acq, count * sizeof(DasBatchAcq)))) return false;
+	if (!cuda_ok(cudaMalloc(&gb.d_counter, sizeof(int)))) return false;
+
+	/* autotuner: every (tile shape, CTAs per SM) candidate runs the batch once to
+	 * warm up and once timed; the fastest is kept */
+	int sms = 152;
+	int dev = 0;
+	if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	const bool tile_choices[2] = {true, false};
+	const int cta_choices[3] = {4, 5, 6};
+	float best = INFINITY;
+	bool best_tiles = true;
+	int best_ctas = 6 * sms;
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	for (int ti = 0; ti < (any_volume ? 2 : 1); ti++) {
+		if (!batch_items(tile_choices[ti])) return false;
+		for (int ci = 0; ci < 3; ci++) {
+			gb.ctas = cta_choices[ci] * sms;
+			if (!cuda_ok(batch_launch(g.stream))) return false;
+			cudaEventRecord(e0, g.stream);
+			if (!cuda_ok(launch_das_batch(gb.d_acq, gb.d_items, gb.n_items, gb.d_counter, gb.interp, gb.ctas, g.stream)))
+				return false;
+			cudaEventRecord(e1, g.stream);
+			if (!cuda_ok(cudaEventSynchronize(e1))) return false;
+			float ms = 0;
+			cudaEventElapsedTime(&ms, e0, e1);
+			gb.candidate_ms.push_back(ms);
+			if (ms < best) { best = ms; best_tiles = tile_choices[ti]; best_ctas = gb.ctas; }
+		}
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	gb.volume_tiles = best_tiles;
+	gb.ctas = best_ctas;
+	if (!batch_items(best_tiles)) return false;
+
+	/* the whole batch as one graph */
+	cudaGraph_t graph = nullptr;
+	const uint64_t k0 = g_kernel_launches;
+	if (!cuda_ok(cudaStreamBeginCapture(g.stream, cudaStreamCaptureModeThreadLocal))) return false;
+	const cudaError_t le = batch_launch(g.stream);
+	const cudaError_t ce = cudaStreamEndCapture(g.stream, &graph);
+	if (!cuda_ok(le) || !cuda_ok(ce)) return false;
+	gb.graph_kernels = g_kernel_launches - k0;
+	g_kernel_launches = k0;
+	const cudaError_t ie = cudaGraphInstantiate(&gb.exec, graph, 0);
+	cudaGraphDestroy(graph);
+	if (!cuda_ok(ie)) return false;
+	gb.signature = batch_signature(params, count, rf, rf_size, out);
+	return true;
 }
 
 } /* namespace */
@@ -1243,6 +1559,7 @@ LIB_FN void beamformer_gb300_shutdown(void)
 {
 	if (!g.ready) return;
 	cudaDeviceSynchronize();
+	free_batch();
 	for (auto &f : g.frames) free_frame(f);
 	for (auto &f : g.averaged) free_frame(f);
 	for (int i = 0; i < RF_SLOTS; i++) {
@@ -1279,6 +1596,46 @@ LIB_FN void beamformer_gb300_shutdown(void)
 	fresh.interpolation_override = g.interpolation_override;
 	fresh.precision = g.precision;
 	g = fresh;
+}
+
+
+LIB_FN uint32_t beamformer_gb300_beamform_batch(const BeamformerParameters *parameters, uint32_t count,
+                                                const void *const *rf, const uint64_t *rf_size, float *const *out,
+                                                int32_t timeout_ms)
+{
+	if (!parameters || !rf || !rf_size || !out || count == 0) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	if (g.shader_count <= 0) return fail(BF_LIB_ERR_KIND_INVALID_COMPUTE_STAGE);
+	if (g.precision != 0) return fail(BF_LIB_ERR_KIND_UNSUPPORTED);
+	for (uint32_t i = 0; i < count; i++)
+		if (!rf[i] || !out[i]) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	if (!ensure_cuda()) return 0;
+	if (gb.signature != batch_signature(parameters, count, rf, rf_size, out) || !gb.exec) {
+		if (!build_batch(parameters, count, rf, rf_size, out)) {
+			free_batch();
+			return 0;
+		}
+	}
+	if (!cuda_ok(cudaGraphLaunch(gb.exec, g.stream))) return 0;
+	g_kernel_launches += gb.graph_kernels;
+	if (!cuda_ok(cudaEventRecord(g.ext_done, g.stream))) return 0;
+	g.last_done = g.ext_done;
+	if (!wait_event(g.ext_done, timeout_ms)) return fail(BF_LIB_ERR_KIND_SYNC_VARIABLE);
+	return 1;
+}
+
+LIB_FN uint32_t beamformer_gb300_batch_tuning(int32_t *volume_tiles, int32_t *ctas, float *candidate_ms,
+                                              int32_t capacity, int32_t *count_out)
+{
+	if (!gb.exec) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	if (volume_tiles) *volume_tiles = gb.volume_tiles ? 1 : 0;
+	if (ctas) *ctas = gb.ctas;
+	const int32_t n = (int32_t)gb.candidate_ms.size();
+	if (count_out) *count_out = n;
+	if (candidate_ms) {
+		if (capacity < n) return fail(BF_LIB_ERR_KIND_BUFFER_OVERFLOW);
+		std::memcpy(candidate_ms, gb.candidate_ms.data(), (size_t)n * sizeof(float));
+	}
+	return 1;
 }
 
 } /* extern "C" */

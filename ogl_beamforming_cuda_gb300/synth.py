@@ -148,3 +148,22 @@ def acquisition(bp, seed, n_points=20, n_speckle=0, device="cpu"):
     pos, amp = scatterers(seed, n_points, n_speckle)
     x = decoded_traces(bp, pos, amp, device=device)
     return encode_and_quantise(x, seed).cpu().numpy()
+
+
+BATCH_GRIDS = ((64, 1, 64), (128, 1, 128), (64, 64, 128), (128, 128, 256))
+
+
+def batch_workload(seed, count=32, transmits=(32, 64, 128), samples=(1024, 2048, 4096), grids=BATCH_GRIDS,
+                   modes=("HERCULES", "FORCES"), interpolate=1, filter_length=64):
+    """Seeded mixed batch: per acquisition a transmit count, sample count, output
+    grid and DAS mode drawn uniformly from the given sets (128 receive channels)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        T = int(rng.choice(transmits))
+        S = int(rng.choice(samples))
+        grid = tuple(grids[int(rng.integers(len(grids)))])
+        mode = str(rng.choice(modes))
+        out.append(make_parameters(samples=S, channels=128, transmits=T, points=grid, decimation=2,
+                                   interpolate=interpolate, das_id=mode, filter_length=filter_length))
+    return out
