@@ -55,6 +55,9 @@ def parse():
                     help="only push this many copies of one device-resident frame through the pipeline "
                          "(for a profiler), print per-stage ms and exit")
     ap.add_argument("--points", default=",".join(map(str, POINTS)), help="voxel grid for --profile-frames")
+    ap.add_argument("--variant", default="plain", choices=["plain", "precision", "batched"],
+                    help="plain: the 3D pipeline (default, the headline line); precision: the FP16/BF16 front end "
+                         "on the 4096-sample plane; batched: 32 mixed acquisitions in one call")
     return ap.parse_args()
 
 
@@ -352,6 +355,144 @@ def cpu_sample(budget_s=12.0):
             "seconds_per_volume": t_volume}
 
 
+def _events_ms(fn, stream, reps):
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def run_precision(args, peaks):
+    """Precision variant on its workload: HERCULES plane 128 x 128, 4096 int16
+    samples, 128-tap FIR, decimation 2, linear DAS; frames/s of the whole
+    pipeline per arithmetic and each stage's error against the FP64 oracle."""
+    import torch
+    from ogl_beamforming_cuda_gb300 import synth, abi
+    from ogl_beamforming_cuda_gb300.client import Beamformer
+    torch.cuda.set_device(0)
+    SH = abi.SHADER
+    pts = (128, 1, 128)
+    bp = synth.make_parameters(samples=4096, points=pts, decimation=2, interpolate=0, frames=1, filter_length=128)
+    kaiser = synth.kaiser_spec(128)
+    pipe = [SH["Decode"], SH["Demodulate"], SH["DAS"]]
+    raw = torch.from_numpy(synth.acquisition(bp, 1, n_points=20, n_speckle=2000, device="cuda:0")).cuda()
+    res = {}
+    for prec, name in ((0, "fp32"), (1, "fp16"), (2, "bf16")):
+        bf = Beamformer().configure(bp, pipe, kaiser=kaiser, interpolation=2)
+        assert bf.lib.beamformer_gb300_set_filter_precision(prec)
+        stream = torch.cuda.ExternalStream(bf.lib.beamformer_gb300_get_stream())
+        push = lambda: bf.push_device(raw.data_ptr(), raw.numel() * 2)
+        for _ in range(max(args.warmup, 3)):
+            push()
+        bf.synchronize()
+        ms = _events_ms(push, stream, max(args.steps, 1) * 20)
+        res[name] = {"frames_per_s": 1e3 / ms, "ms_per_frame": ms, "stage_ms": {k: v * 1e3 for k, v in
+                                                                                stage_times(bf, 20).items()},
+                     "channel_data": bf.channel_data().copy(), "frame": bf.frame(0)[0].copy(), "bf": bf}
+    errors = None
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import ctypes
+        import oracle.bf_oracle as O
+        from bf_cases import oracle_for
+        orc = oracle_for(res["fp32"]["bf"], bp, pipe, kaiser=kaiser)
+        orc.interpolation = 2
+        ref = orc.compute(raw.cpu().numpy(), want_stages=True)
+        p = ref["plan"]
+        dec = ref["stages"][0][1].astype(np.float64)
+        dem = np.zeros_like(dec)
+        taps = O.kaiser_f64(kaiser[1], kaiser[2], kaiser[0], kaiser[3])
+        O.lib().bfo_filter_f64(ctypes.byref(p.demod), SH["DemodulateFloat"], O._ptr(dec), dec.size, O._ptr(dem),
+                               dem.size, O._arr(taps, ctypes.c_double), kaiser[3], p.demod_dispatch, O.threads())
+        n = 2 * int(p.demod.output_channel_stride) * C
+        vol = O.das(p.das, dem[: p.rf_size // 4], pts, orc.sparse, orc.focal, fast=True, interpolation=2, f64=True)
+
+        def db(a, b):
+            return float(20 * np.log10(np.sqrt(np.mean((a - b) ** 2) / np.mean(b ** 2))))
+        errors = {k: {"demod_db_vs_fp64": db(v["channel_data"][:n], dem[:n]), "volume_db_vs_fp64": db(v["frame"], vol)}
+                  for k, v in res.items()}
+    for v in res.values():
+        for k in ("channel_data", "frame", "bf"):
+            v.pop(k)
+    print(json.dumps({
+        "metric": "frames/s of the precision variant (decode + demodulate + DAS, plane)", "variant": "precision",
+        "value": res["bf16"]["frames_per_s"], "unit": "frames/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "higher_is_better": True, "dtype": "fp16/bf16 operands, f32 accumulate",
+        "data": "synthetic (seeded RF generator)",
+        "config": {"workload": "HERCULES plane 128x1x128, 128 tx, 128 rx, 4096 int16 samples, 128-tap Kaiser, "
+                               "decimation 2, linear DAS", "l2": "one 134 MB frame per push, larger than L2"},
+        "per_precision": res, "errors": errors,
+        "speedup_vs_fp32": {k: res[k]["frames_per_s"] / res["fp32"]["frames_per_s"] for k in res}}))
+    return 0
+
+
+def run_batched(args, peaks):
+    """Batched variant: 32 seeded acquisitions (transmits {32, 64, 128}, samples
+    {1024, 2048, 4096}, grids from 64x64 planes to 128x128x256 volumes,
+    HERCULES or FORCES), cubic DAS, beamformed by one batch call (graph replay)
+    against the same acquisitions pushed one at a time through the plain API."""
+    import torch
+    from ogl_beamforming_cuda_gb300 import synth, abi
+    from ogl_beamforming_cuda_gb300.client import Beamformer
+    torch.cuda.set_device(0)
+    SH = abi.SHADER
+    pipe = [SH["Decode"], SH["Demodulate"], SH["DAS"]]
+    kaiser = synth.kaiser_spec(64)
+    params = synth.batch_workload(7, count=32, interpolate=1)
+    rf, out = [], []
+    for i, bp in enumerate(params):
+        rf.append(torch.from_numpy(synth.acquisition(bp, 500 + i, n_points=20, n_speckle=200, device="cuda:0")).cuda())
+        out.append(torch.zeros(2 * int(np.prod(list(bp.output_points)[:3])), dtype=torch.float32, device="cuda:0"))
+    bf = Beamformer().configure(params[0], pipe, kaiser=kaiser, interpolation=1)
+    stream = torch.cuda.ExternalStream(bf.lib.beamformer_gb300_get_stream())
+    bargs = (params, [t.data_ptr() for t in rf], [t.numel() * 2 for t in rf], [t.data_ptr() for t in out])
+    t0 = time.perf_counter()
+    bf.beamform_batch(*bargs)
+    build_s = time.perf_counter() - t0
+    for _ in range(max(args.warmup, 3) - 1):
+        bf.beamform_batch(*bargs)
+    l0 = bf.launches()
+    reps = max(args.steps, 1)
+    ms_batch = _events_ms(lambda: bf.beamform_batch(*bargs), stream, reps)
+    launches = (bf.launches() - l0) // reps
+    tiles, ctas, cand = bf.batch_tuning()
+    # the same acquisitions one at a time through the plain pipeline (re-planned per acquisition)
+    single = Beamformer().configure(params[0], pipe, kaiser=kaiser, interpolation=1)
+
+    def one_by_one():
+        for bp, t in zip(params, rf):
+            single.configure(bp, pipe, kaiser=kaiser, interpolation=1)
+            single.push_device(t.data_ptr(), t.numel() * 2)
+    one_by_one()
+    single.synchronize()
+    h0 = time.perf_counter()
+    one_by_one()
+    single.synchronize()
+    ms_single = (time.perf_counter() - h0) * 1e3
+    vox = [int(np.prod(list(bp.output_points)[:3])) for bp in params]
+    print(json.dumps({
+        "metric": "volumes/s of 32 mixed acquisitions, batched vs one at a time", "variant": "batched",
+        "value": 32 / (ms_batch / 1e3), "unit": "volumes/s", "n_gpus": 1, "steps": reps, "warmup": args.warmup,
+        "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded RF generator)",
+        "config": {"workload": "32 acquisitions: transmits {32,64,128}, samples {1024,2048,4096}, grids "
+                               "{64x1x64, 128x1x128, 64x64x128, 128x128x256}, HERCULES or FORCES, 128 rx, cubic DAS",
+                   "acquisitions": [{"T": int(bp.dec_data_dim[2]), "S": int(bp.dec_data_dim[0]),
+                                     "grid": list(bp.output_points)[:3], "das": int(bp.das_shader_id)} for bp in params],
+                   "total_voxels": int(sum(vox))},
+        "ms_per_batch": ms_batch, "gpu_launches_per_batch": launches,
+        "one_at_a_time": {"ms_per_batch": ms_single, "volumes_per_s": 32 / (ms_single / 1e3),
+                          "how": "configure + push_device per acquisition (the plain API), host-timed"},
+        "speedup_vs_one_at_a_time": ms_single / ms_batch,
+        "autotuner": {"volume_tiles": tiles, "ctas": ctas, "candidate_ms": [float(x) for x in cand],
+                      "first_call_s": build_s}}))
+    return 0
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -360,6 +501,10 @@ def main():
     peaks = measured_peaks()
     if args.profile_frames > 0:
         return profile_frames(args)
+    if args.variant == "precision":
+        return run_precision(args, peaks)
+    if args.variant == "batched":
+        return run_batched(args, peaks)
 
     if args.impl == "reference":
         if rank != 0:

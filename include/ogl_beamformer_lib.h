@@ -348,7 +348,9 @@ LIB_FN uint32_t beamformer_gb300_set_filter_precision(int32_t precision);
  * elements, focal vectors and interpolation; the pipeline's last stage must be DAS
  * without coherency weighting, the DAS modes HERCULES (not sparse) or FORCES, and
  * all acquisitions must use one interpolation mode. The front ends run per
- * acquisition and the DAS of all acquisitions runs as one persistent launch; on
+ * acquisition and the DAS of all acquisitions runs as persistent launches that
+ * take voxel tiles from cost-ordered work lists (one launch for the HERCULES
+ * tiles, one for the FORCES tiles, per 64 acquisitions); on
  * the first call for a set of parameters and pointers the tile shape and grid
  * size are autotuned on the device and the whole batch is captured in a CUDA graph,
  * which later calls with the same set replay. timeout_ms as

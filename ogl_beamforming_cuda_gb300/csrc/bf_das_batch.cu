@@ -7,10 +7,13 @@
  * output grid and DAS mode. Their voxel tiles form one work list, ordered by
  * estimated cost (largest first); a grid of a few CTAs per SM takes tiles from
  * it with an atomic counter until it is empty, so small planes run beside large
- * volumes and no SM idles while work remains. A CTA copies the parameters of its
- * tile's acquisition into shared memory and runs the same per-tile code as the
- * single-acquisition kernels: the HERCULES fast path (bf_das_hercules.cuh) with
- * volume or plane tiles, or the general path (bf_das_generic.cuh) for FORCES.
+ * volumes and no SM idles while work remains. The acquisitions' parameters travel
+ * by value in the kernel's parameter space (up to DAS_BATCH_MAX per launch), so a
+ * tile reads them through the constant cache as a single launch does, and runs
+ * the same per-tile code as the single-acquisition kernels: the HERCULES fast
+ * path (bf_das_hercules.cuh) with volume or plane tiles, or the general path
+ * (bf_das_generic.cuh) for FORCES. The two paths are two persistent launches
+ * with their own work lists, so each keeps its own register budget.
  * Every voxel of every acquisition is written once, in the same arithmetic and
  * accumulation order as the single-acquisition launch.
  */
@@ -21,45 +24,35 @@
 
 namespace bf {
 
-template <int INTERP>
-__global__ void __launch_bounds__(DAS_THREADS, 6)
-das_batch(const DasBatchAcq *__restrict__ acq, const int4 *__restrict__ items, int n_items, int *next)
+/* GENERAL = false: HERCULES tiles (up to 80 registers, 6 CTAs per SM); true:
+ * tiles of the general path (FORCES), compiled on their own (64 registers, 8
+ * CTAs per SM) with their parameters copied to registers per tile. */
+template <int INTERP, bool GENERAL>
+__global__ void __launch_bounds__(DAS_THREADS, GENERAL ? 8 : 6)
+das_batch(const __grid_constant__ DasBatchArgs args, const int4 *__restrict__ items, int n_items, int *next)
 {
-	__shared__ DasParams sp;
-	__shared__ const float4 *stab;
-	__shared__ int spath, sitem, sacq;
-	if (threadIdx.x == 0) sacq = -1;
-	constexpr int WORDS = (int)(sizeof(DasParams) / 4);
+	__shared__ int sitem;
 	while (true) {
-		__syncthreads();                        /* the previous tile is done with sp and sitem */
+		__syncthreads();                        /* every thread has read the previous item */
 		if (threadIdx.x == 0) sitem = atomicAdd(next, 1);
 		__syncthreads();
 		const int it = sitem;
 		if (it >= n_items) return;              /* uniform over the CTA */
 		const int4 w = __ldg(items + it);
-		if (w.x != sacq) {
-			__syncthreads();                    /* every thread has read sacq */
-			const uint32_t *src = (const uint32_t *)&acq[w.x].p;
-			for (int k = threadIdx.x; k < WORDS; k += blockDim.x) ((uint32_t *)&sp)[k] = __ldg(src + k);
-			if (threadIdx.x == 0) {
-				stab = acq[w.x].table;
-				spath = acq[w.x].path;
-				sacq = w.x;
-			}
-			__syncthreads();
-		}
-		const int path = spath;
-		if (path == DAS_BATCH_HERC_VOLUME) {
-			hercules_tile<INTERP, 4>(sp, stab, w.y, w.z, w.w, 0);
-		} else if (path == DAS_BATCH_HERC_PLANE) {
-			hercules_tile<INTERP, 1>(sp, stab, w.y, w.z, w.w, 0);
+		const DasBatchAcq &a = args.acq[w.x];
+		if (!GENERAL) {
+			if (a.path == DAS_BATCH_HERC_VOLUME) hercules_tile<INTERP, 4>(a.p, a.table, w.y, w.z, w.w, 0);
+			else                                 hercules_tile<INTERP, 1>(a.p, a.table, w.y, w.z, w.w, 0);
 		} else {
 			const int vx = w.y * DAS_TX + (int)(threadIdx.x & (DAS_TX - 1));
 			const int vz = w.w * DAS_TZ + (int)(threadIdx.x / DAS_TX);
 			const int vy = w.z;
-			if (vx < sp.dims[0] && vz < sp.dims[2]) {
-				const float2 v = das_voxel<DAS_FORCES, INTERP, true>(sp, vx, vy, vz, 0, sp.loop_end);
-				sp.frame[((int64_t)vz * sp.dims[1] + vy) * sp.dims[0] + vx] = v;
+			/* a register copy: the loop then reads its constants from registers, not
+			 * through a runtime-indexed parameter load per use */
+			const DasParams p = a.p;
+			if (vx < p.dims[0] && vz < p.dims[2]) {
+				const float2 v = das_voxel<DAS_FORCES, INTERP, true>(p, vx, vy, vz, 0, p.loop_end);
+				p.frame[((int64_t)vz * p.dims[1] + vy) * p.dims[0] + vx] = v;
 			}
 		}
 	}
@@ -83,17 +76,20 @@ void das_batch_tiles(const DasParams &p, int path, int tiles[3])
 	}
 }
 
-cudaError_t launch_das_batch(const DasBatchAcq *acq, const int4 *items, int n_items, int *counter, int interp,
-                             int ctas, cudaStream_t s)
+cudaError_t launch_das_batch(const DasBatchArgs &args, const int4 *items, int n_items, int *counter, int interp,
+                             bool general, int ctas, cudaStream_t s)
 {
 	if (n_items <= 0) return cudaSuccess;
 	cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), s);
 	if (e != cudaSuccess) return e;
+#define BF_BATCH(I) (general ? das_batch<I, true><<<ctas, DAS_THREADS, 0, s>>>(args, items, n_items, counter) \
+                             : das_batch<I, false><<<ctas, DAS_THREADS, 0, s>>>(args, items, n_items, counter))
 	switch (interp) {
-	case INTERP_CUBIC:  das_batch<INTERP_CUBIC><<<ctas, DAS_THREADS, 0, s>>>(acq, items, n_items, counter); break;
-	case INTERP_LINEAR: das_batch<INTERP_LINEAR><<<ctas, DAS_THREADS, 0, s>>>(acq, items, n_items, counter); break;
-	default:            das_batch<INTERP_NEAREST><<<ctas, DAS_THREADS, 0, s>>>(acq, items, n_items, counter); break;
+	case INTERP_CUBIC:  BF_BATCH(INTERP_CUBIC); break;
+	case INTERP_LINEAR: BF_BATCH(INTERP_LINEAR); break;
+	default:            BF_BATCH(INTERP_NEAREST); break;
 	}
+#undef BF_BATCH
 	g_kernel_launches++;
 	return cudaGetLastError();
 }

@@ -140,10 +140,16 @@ struct DasBatchAcq {
 	int32_t       path;        /* DasBatchPath */
 	int32_t       reserved;
 };
+/* up to DAS_BATCH_MAX acquisitions per launch, passed by value in the kernel's
+ * parameter space (read through the constant cache, like a single launch's) */
+constexpr int DAS_BATCH_MAX = 64;
+struct DasBatchArgs {
+	DasBatchAcq acq[DAS_BATCH_MAX];
+};
 /* tile grid of an acquisition on a path; work items are int4 (acquisition, tile x, y, z) */
 void        das_batch_tiles(const DasParams &p, int path, int tiles[3]);
-cudaError_t launch_das_batch(const DasBatchAcq *acq, const int4 *items, int n_items, int *counter, int interp,
-                             int ctas, cudaStream_t s);
+cudaError_t launch_das_batch(const DasBatchArgs &args, const int4 *items, int n_items, int *counter, int interp,
+                             bool general, int ctas, cudaStream_t s);
 /* the per-frame HERCULES interpolation table alone (cubic / linear; nothing for nearest) */
 cudaError_t launch_das_table(const DasParams &p, float4 *table, cudaStream_t s);
 

@@ -26,6 +26,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <thread>
 #include <vector>
 
@@ -909,16 +910,23 @@ struct BatchAcqState {
 	uint64_t    rf_bytes = 0;
 };
 
+/* Acquisitions [first, first + count) of a batch: one persistent DAS launch. */
+struct BatchChunk {
+	int                           first = 0, count = 0;
+	std::unique_ptr<DasBatchArgs> args;
+	int4                         *d_items[2] = {nullptr, nullptr};   /* HERCULES tiles, general-path tiles */
+	size_t                        items_cap[2] = {0, 0};
+	int                           n_items[2] = {0, 0};
+	int                          *d_counter = nullptr;              /* two counters */
+};
+
 struct BatchState {
 	uint64_t                   signature = 0;
 	std::vector<BatchAcqState> acq;
-	DasBatchAcq               *d_acq = nullptr;
-	int4                      *d_items = nullptr;
-	size_t                     items_cap = 0;
-	int                       *d_counter = nullptr;
-	int                        n_items = 0;
+	std::vector<BatchChunk>    chunks;
 	int                        interp = INTERP_NEAREST;
-	int                        ctas = 0;
+	int                        ctas = 0;             /* persistent CTAs of the HERCULES launch */
+	int                        ctas_general = 0;     /* and of the general-path launch */
 	bool                       volume_tiles = true;
 	cudaGraphExec_t            exec = nullptr;
 	uint64_t                   graph_kernels = 0;
@@ -937,9 +945,11 @@ void free_batch()
 		cudaFree(a.das_table);
 		cudaFree(a.hadamard);
 	}
-	cudaFree(gb.d_acq);
-	cudaFree(gb.d_items);
-	cudaFree(gb.d_counter);
+	for (auto &c : gb.chunks) {
+		cudaFree(c.d_items[0]);
+		cudaFree(c.d_items[1]);
+		cudaFree(c.d_counter);
+	}
 	gb = BatchState();
 }
 
@@ -971,8 +981,20 @@ uint64_t batch_signature(const BeamformerParameters *params, uint32_t count, con
 	return h;
 }
 
+/* The persistent DAS launch of every chunk. */
+cudaError_t batch_das(cudaStream_t s)
+{
+	for (auto &c : gb.chunks) {
+		cudaError_t e = launch_das_batch(*c.args, c.d_items[0], c.n_items[0], c.d_counter, gb.interp, false, gb.ctas, s);
+		if (e != cudaSuccess) return e;
+		e = launch_das_batch(*c.args, c.d_items[1], c.n_items[1], c.d_counter + 1, gb.interp, true, gb.ctas_general, s);
+		if (e != cudaSuccess) return e;
+	}
+	return cudaSuccess;
+}
+
 /* Front end (decode / demodulate / filter stages) of every acquisition, the
- * HERCULES interpolation tables, then the one persistent DAS launch. */
+ * HERCULES interpolation tables, then the persistent DAS launch. */
 cudaError_t batch_launch(cudaStream_t s)
 {
 	for (auto &a : gb.acq) {
@@ -1001,43 +1023,52 @@ cudaError_t batch_launch(cudaStream_t s)
 			if (e != cudaSuccess) return e;
 		}
 	}
-	return launch_das_batch(gb.d_acq, gb.d_items, gb.n_items, gb.d_counter, gb.interp, gb.ctas, s);
+	return batch_das(s);
 }
 
-/* Paths and the cost-ordered work list for a tile choice; uploads both. */
+/* Paths and the cost-ordered work lists (one per chunk of up to DAS_BATCH_MAX
+ * acquisitions) for a tile choice; uploads the lists. */
 bool batch_items(bool volume_tiles)
 {
-	std::vector<DasBatchAcq> acqs(gb.acq.size());
-	struct Entry { double cost; int acq; };
-	std::vector<Entry> order;
-	for (size_t i = 0; i < gb.acq.size(); i++) {
-		BatchAcqState &a = gb.acq[i];
-		if (a.das.family == DAS_HERCULES)
-			a.path = volume_tiles && a.das.dims[1] >= 4 ? DAS_BATCH_HERC_VOLUME : DAS_BATCH_HERC_PLANE;
-		acqs[i].p = a.das;
-		acqs[i].table = a.das_table;
-		acqs[i].path = a.path;
-		const double vox = a.path == DAS_BATCH_HERC_VOLUME ? 256.0 : 128.0;
-		order.push_back({vox * a.das.T * a.das.C, (int)i});
+	for (auto &c : gb.chunks) {
+		struct Entry { double cost; int acq; };
+		std::vector<Entry> order;
+		for (int k = 0; k < c.count; k++) {
+			BatchAcqState &a = gb.acq[(size_t)(c.first + k)];
+			if (a.das.family == DAS_HERCULES)
+				a.path = volume_tiles && a.das.dims[1] >= 4 ? DAS_BATCH_HERC_VOLUME : DAS_BATCH_HERC_PLANE;
+			DasBatchAcq &d = c.args->acq[k];
+			d.p = a.das;
+			d.table = a.das_table;
+			d.path = a.path;
+			const double vox = a.path == DAS_BATCH_HERC_VOLUME ? 256.0 : 128.0;
+			order.push_back({vox * a.das.T * a.das.C, k});
+		}
+		std::stable_sort(order.begin(), order.end(), [](const Entry &x, const Entry &y) { return x.cost > y.cost; });
+		std::vector<int4> items[2];
+		for (const Entry &e : order) {
+			int tiles[3];
+			const int path = c.args->acq[e.acq].path;
+			das_batch_tiles(c.args->acq[e.acq].p, path, tiles);
+			std::vector<int4> &list = items[path == DAS_BATCH_GENERIC ? 1 : 0];
+			for (int z = 0; z < tiles[2]; z++)
+				for (int y = 0; y < tiles[1]; y++)
+					for (int x = 0; x < tiles[0]; x++) list.push_back(make_int4(e.acq, x, y, z));
+		}
+		for (int l = 0; l < 2; l++) {
+			if (items[l].size() > c.items_cap[l]) {
+				cudaFree(c.d_items[l]);
+				c.d_items[l] = nullptr;
+				if (!cuda_ok(cudaMalloc(&c.d_items[l], items[l].size() * sizeof(int4)))) return false;
+				c.items_cap[l] = items[l].size();
+			}
+			c.n_items[l] = (int)items[l].size();
+			if (c.n_items[l] && !cuda_ok(cudaMemcpy(c.d_items[l], items[l].data(), items[l].size() * sizeof(int4),
+			                                         cudaMemcpyHostToDevice)))
+				return false;
+		}
 	}
-	std::stable_sort(order.begin(), order.end(), [](const Entry &x, const Entry &y) { return x.cost > y.cost; });
-	std::vector<int4> items;
-	for (const Entry &e : order) {
-		int tiles[3];
-		das_batch_tiles(gb.acq[e.acq].das, gb.acq[e.acq].path, tiles);
-		for (int z = 0; z < tiles[2]; z++)
-			for (int y = 0; y < tiles[1]; y++)
-				for (int x = 0; x < tiles[0]; x++) items.push_back(make_int4(e.acq, x, y, z));
-	}
-	if (items.size() > gb.items_cap) {
-		cudaFree(gb.d_items);
-		gb.d_items = nullptr;
-		if (!cuda_ok(cudaMalloc(&gb.d_items, items.size() * sizeof(int4)))) return false;
-		gb.items_cap = items.size();
-	}
-	gb.n_items = (int)items.size();
-	if (!cuda_ok(cudaMemcpy(gb.d_items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice))) return false;
-	return cuda_ok(cudaMemcpy(gb.d_acq, acqs.data(), acqs.size() * sizeof(DasBatchAcq), cudaMemcpyHostToDevice));
+	return true;
 }
 
 /* Plans, buffers and tables of a new batch; autotunes the DAS launch (tile
@@ -1107,8 +1138,14 @@ bool build_batch(const BeamformerParameters *params, uint32_t count, const void 
 		interp = a.das.interp;
 	}
 	gb.interp = interp;
-	if (!cuda_ok(cudaMalloc(&gb.d_acq, count * sizeof(DasBatchAcq)))) return false;
-	if (!cuda_ok(cudaMalloc(&gb.d_counter, sizeof(int)))) return false;
+	for (uint32_t first = 0; first < count; first += DAS_BATCH_MAX) {
+		BatchChunk c;
+		c.first = (int)first;
+		c.count = (int)std::min<uint32_t>(count - first, DAS_BATCH_MAX);
+		c.args.reset(new DasBatchArgs());
+		if (!cuda_ok(cudaMalloc(&c.d_counter, 2 * sizeof(int)))) return false;
+		gb.chunks.push_back(std::move(c));
+	}
 
 	/* autotuner: every (tile shape, CTAs per SM) candidate runs the batch once to
 	 * warm up and once timed; the fastest is kept */
@@ -1117,6 +1154,7 @@ bool build_batch(const BeamformerParameters *params, uint32_t count, const void 
 	if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
 	const bool tile_choices[2] = {true, false};
 	const int cta_choices[3] = {4, 5, 6};
+	gb.ctas_general = 8 * sms;
 	float best = INFINITY;
 	bool best_tiles = true;
 	int best_ctas = 6 * sms;
@@ -1129,8 +1167,7 @@ bool build_batch(const BeamformerParameters *params, uint32_t count, const void 
 			gb.ctas = cta_choices[ci] * sms;
 			if (!cuda_ok(batch_launch(g.stream))) return false;
 			cudaEventRecord(e0, g.stream);
-			if (!cuda_ok(launch_das_batch(gb.d_acq, gb.d_items, gb.n_items, gb.d_counter, gb.interp, gb.ctas, g.stream)))
-				return false;
+			if (!cuda_ok(batch_das(g.stream))) return false;
 			cudaEventRecord(e1, g.stream);
 			if (!cuda_ok(cudaEventSynchronize(e1))) return false;
 			float ms = 0;
