@@ -311,8 +311,9 @@ LIB_FN uint32_t beamformer_gb300_synchronize(int32_t timeout_ms);
 /* Copy a frame out of the device frame store: which = 0 latest beamformed
  * frame, 1 latest averaged frame (written by the Sum stage). mip_level selects
  * the Min/Max pyramid level (0 = the frame itself). Output is 2 floats per
- * point in x-fastest order; out_size is in bytes. The reference keeps these
- * levels in GL textures (beamformer.c:119-151, 595-607). */
+ * point in x-fastest order; out_size is in bytes; out may be host or device
+ * memory. The reference keeps these levels in GL textures (beamformer.c:119-151,
+ * 595-607). */
 LIB_FN uint32_t beamformer_gb300_export_frame(uint32_t which, uint32_t mip_level, float *out,
                                               uint64_t out_size, int32_t dims_out[3]);
 
@@ -338,6 +339,12 @@ LIB_FN uint32_t beamformer_gb300_set_interpolation(int32_t mode);
  * later stages stay FP32. Other pipelines fail with UNSUPPORTED at compute time
  * while a 16-bit precision is selected. Takes effect at the next compute. */
 LIB_FN uint32_t beamformer_gb300_set_filter_precision(int32_t precision);
+
+/* Receive-aperture subsampling of HERCULES delay-and-sum (no counterpart in the
+ * reference; the input of the learned variant): DAS sums receive channels 0,
+ * step, 2 step, ... only (step 1, the default, uses all). Other DAS modes fail
+ * with UNSUPPORTED while step > 1. Takes effect at the next compute. */
+LIB_FN uint32_t beamformer_gb300_set_receive_subsampling(int32_t step);
 
 /* Beamform `count` acquisitions in one go (the batched variant; no counterpart
  * in the reference, which beamforms one acquisition per compute). Acquisition i

@@ -21,7 +21,7 @@ NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 INC = [f"-I{os.path.join(ROOT, 'include')}", f"-I{CSRC}"]
 
-CU = ["bf_decode.cu", "bf_filter.cu", "bf_fir_tc.cu", "bf_das.cu", "bf_das_hercules.cu", "bf_das_batch.cu", "bf_reduce.cu"]
+CU = ["bf_decode.cu", "bf_filter.cu", "bf_fir_tc.cu", "bf_das.cu", "bf_das_hercules.cu", "bf_das_batch.cu", "bf_reduce.cu", "bf_unet.cu"]
 CPP = ["bf_host.cpp", "bf_library.cpp"]
 HEADERS = ["bf_kernels.h", "bf_host.h", "bf_das_math.cuh", "bf_das_generic.cuh", "bf_das_hercules.cuh"]
 
@@ -30,7 +30,7 @@ def _stale(obj, src):
     if not os.path.exists(obj):
         return True
     t = os.path.getmtime(obj)
-    deps = [src] + [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "ogl_beamformer_lib.h")]
+    deps = [src] + [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "ogl_beamformer_lib.h"), os.path.join(ROOT, "include", "bf_unet.h")]
     return any(os.path.getmtime(d) > t for d in deps)
 
 

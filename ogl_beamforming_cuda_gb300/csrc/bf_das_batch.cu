@@ -80,6 +80,8 @@ cudaError_t launch_das_batch(const DasBatchArgs &args, const int4 *items, int n_
                              bool general, int ctas, cudaStream_t s)
 {
 	if (n_items <= 0) return cudaSuccess;
+	for (int i = 0; i < DAS_BATCH_MAX; i++)
+		if (args.acq[i].p.frame && args.acq[i].p.rx_step < 1) return cudaErrorInvalidValue;
 	cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), s);
 	if (e != cudaSuccess) return e;
 #define BF_BATCH(I) (general ? das_batch<I, true><<<ctas, DAS_THREADS, 0, s>>>(args, items, n_items, counter) \

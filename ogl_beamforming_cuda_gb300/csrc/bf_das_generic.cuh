@@ -172,7 +172,7 @@ __device__ __forceinline__ float2 das_voxel(const DasParams &p, int vx, int vy, 
 			/* receive channel r fixes one lateral coordinate, transmit t the other */
 			const float q_fix = p.rx_cols ? q[0] : q[1], pitch_fix = p.rx_cols ? p.px : p.py;
 			const float q_var = p.rx_cols ? q[1] : q[0], pitch_var = p.rx_cols ? p.py : p.px;
-			for (int r = u_begin; r < u_end; r++) {
+			for (int r = u_begin; r < u_end; r += p.rx_step) {
 				const float df = __fsub_rn(q_fix, __fmul_rn((float)r, pitch_fix));
 				const float f2 = __fmul_rn(df, df);
 				int t_lo, t_hi;

@@ -112,7 +112,7 @@ cudaError_t launch_das_hercules(const DasParams &p, float4 *table, cudaStream_t 
 {
 	const int64_t n = (int64_t)p.dims[0] * p.dims[1] * p.dims[2];
 	if (n == 0) return cudaSuccess;
-	if (!das_hercules_supported(p) || p.groups < 1 || (p.groups > 1 && !p.partial) ||
+	if (!das_hercules_supported(p) || p.groups < 1 || (p.groups > 1 && !p.partial) || p.rx_step < 1 ||
 	    (p.interp != INTERP_NEAREST && !table))
 		return cudaErrorInvalidValue;
 	if (p.interp != INTERP_NEAREST) {

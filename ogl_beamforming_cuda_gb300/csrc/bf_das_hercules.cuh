@@ -127,7 +127,7 @@ __device__ __forceinline__ void hercules_column(const DasParams &p, const float4
 	float lim2 = v[0].lim2;
 	#pragma unroll
 	for (int k = 1; k < NV; k++) lim2 = fmaxf(lim2, v[k].lim2);
-	for (int r = u_begin; r < u_end; r++) {
+	for (int r = u_begin; r < u_end; r += p.rx_step) {
 		const float df = __fsub_rn(q_fix, __fmul_rn((float)r, pitch_fix));
 		const float f2 = __fmul_rn(df, df);
 		int t_lo, t_hi;

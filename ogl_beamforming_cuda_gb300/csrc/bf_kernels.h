@@ -98,6 +98,7 @@ struct DasParams {
 	 * IEEE sqrt over [sqrt_lo, sqrt_hi]), 0 = IEEE sqrt */
 	int32_t        fast_sqrt;
 	int32_t        dense_rows;   /* rf holds exactly C*T*S samples (< 2^31), S >= 4: branch-free HERCULES path */
+	int32_t        rx_step;      /* HERCULES: receive channels 0, rx_step, 2 rx_step, ... (1 = all) */
 	float          sqrt_lo, sqrt_hi;
 };
 

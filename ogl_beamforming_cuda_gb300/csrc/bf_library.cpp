@@ -125,6 +125,7 @@ struct Context {
 	/* precision variant: 0 FP32 (reference arithmetic), 1 FP16, 2 BF16 Decode output
 	 * and tensor-core Demodulate FIR */
 	int32_t      precision = 0;
+	int32_t      rx_step = 1;             /* receive subsampling of HERCULES DAS (learned variant input) */
 	bool         tc_active = false;
 	void        *tc_table = nullptr;
 	size_t       tc_table_cap = 0;
@@ -664,6 +665,8 @@ bool fill_das_params(const Plan &pl, int kind, const void *rf, uint64_t rf_bytes
 	}
 	p.groups = 1;
 	p.per_group = p.loop_end;
+	p.rx_step = g.rx_step;
+	if (p.rx_step > 1 && (p.family != DAS_HERCULES || !p.fast || p.sparse_mode)) return fail(BF_LIB_ERR_KIND_UNSUPPORTED), false;
 	return true;
 }
 
@@ -725,6 +728,7 @@ bool run_stage(int i, const void *src, uint64_t src_bytes, DeviceFrame &frame, b
 			int64_t want = (2048 + vblocks - 1) / vblocks;
 			if (want > p.loop_end) want = p.loop_end;
 			p.per_group = (int32_t)((p.loop_end + want - 1) / want);
+			p.per_group = (p.per_group + p.rx_step - 1) / p.rx_step * p.rx_step;   /* groups start on kept channels */
 			p.groups = (p.loop_end + p.per_group - 1) / p.per_group;
 		}
 		if (p.groups > 1) {
@@ -1466,7 +1470,7 @@ LIB_FN uint32_t beamformer_gb300_export_frame(uint32_t which, uint32_t mip_level
 	if (!out) return 1;
 	if (bytes > out_size) return fail(BF_LIB_ERR_KIND_EXPORT_SPACE_OVERFLOW);
 	if (!cuda_ok(cudaStreamSynchronize(g.stream))) return 0;
-	return cuda_ok(cudaMemcpy(out, src, bytes, cudaMemcpyDeviceToHost)) ? 1 : 0;
+	return cuda_ok(cudaMemcpy(out, src, bytes, cudaMemcpyDefault)) ? 1 : 0;    /* host or device out */
 }
 
 LIB_FN uint32_t beamformer_gb300_export_channel_data(void *out, uint64_t out_size, uint64_t *size_out)
@@ -1487,6 +1491,13 @@ LIB_FN uint32_t beamformer_gb300_get_filter(uint8_t slot, float *taps, int32_t c
 	if (!taps) return 1;
 	if (capacity < n) return fail(BF_LIB_ERR_KIND_BUFFER_OVERFLOW);
 	std::memcpy(taps, g.taps[s].data(), (size_t)n * sizeof(float));
+	return 1;
+}
+
+LIB_FN uint32_t beamformer_gb300_set_receive_subsampling(int32_t step)
+{
+	if (step < 1 || step > 256) return fail(BF_LIB_ERR_KIND_UNSUPPORTED);
+	g.rx_step = step;
 	return 1;
 }
 
@@ -1568,6 +1579,7 @@ LIB_FN uint32_t beamformer_gb300_das_no_alloc(const BeamformerParameters *das_pa
 	p.c_hi = p.fs_hi = 0.0f;
 	p.fast_sqrt = 0;
 	p.dense_rows = p.rf_count >= dense && dense < (1ll << 31) && p.S >= 4;
+	p.rx_step = 1;
 	p.groups = 1;
 	p.per_group = p.loop_end;
 	const int64_t vblocks = (int64_t)((p.dims[0] + 7) / 8) * p.dims[1] * ((p.dims[2] + 15) / 16);
@@ -1632,6 +1644,7 @@ LIB_FN void beamformer_gb300_shutdown(void)
 	fresh.timeout_ms = g.timeout_ms;
 	fresh.interpolation_override = g.interpolation_override;
 	fresh.precision = g.precision;
+	fresh.rx_step = g.rx_step;
 	g = fresh;
 }
 

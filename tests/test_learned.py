@@ -1,0 +1,152 @@
+"""Learned variant: the U-Net kernels against the numpy restatement (forward,
+input and weight gradients, pooling, upsampling, loss), the whole network's
+gradient against a float64 reference of the same network, and training on
+pipeline-made pairs improving on the subsampled DAS it starts from."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import unet_ref as U
+
+pytestmark = pytest.mark.gpu
+
+
+def bf16(a):
+    """round to bfloat16 (nearest even), returned as float64"""
+    t = torch.from_numpy(np.asarray(a, np.float32)).to(torch.bfloat16)
+    return t.float().numpy().astype(np.float64)
+
+
+@pytest.fixture(scope="module")
+def k():
+    from ogl_beamforming_cuda_gb300.learned import Kernels
+    torch.cuda.set_device(0)
+    return Kernels()
+
+
+def dev(a, dtype):
+    return torch.from_numpy(np.asarray(a, np.float32)).to(device="cuda", dtype=dtype).contiguous()
+
+
+def rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-30))
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-30))
+
+
+@pytest.mark.parametrize("cin,cout,dims,relu", [(5, 11, (40, 12, 10), True), (16, 8, (32, 8, 8), False),
+                                                (2, 16, (24, 20, 9), True)])
+def test_conv_forward(k, cin, cout, dims, relu):
+    rng = np.random.default_rng(cin * 100 + cout)
+    W, H, D = dims
+    x = bf16(rng.standard_normal((cin, D, H, W)))
+    w = bf16(rng.standard_normal((cout, cin, 27)) * 0.2)
+    b = rng.standard_normal(cout).astype(np.float32)
+    r = rng.standard_normal((cout, D, H, W)).astype(np.float32)
+    out = torch.empty((cout, D, H, W), dtype=torch.float32, device="cuda")
+    k.conv(dev(x, torch.bfloat16), cin, dev(w.ravel(), torch.bfloat16), dev(b, torch.float32), out, cout, dims, relu,
+           residual=dev(r, torch.float32))
+    ref = U.conv3d(x, w, b, relu=relu, residual=r)
+    assert rel(out.cpu().numpy(), ref) < 2e-6
+
+
+def test_conv_grad_input(k):
+    rng = np.random.default_rng(7)
+    cin, cout, dims = 12, 9, (33, 10, 11)
+    W, H, D = dims
+    g = rng.standard_normal((cout, D, H, W)).astype(np.float32)
+    w = bf16(rng.standard_normal((cout, cin, 27)) * 0.2)
+    out = torch.empty((cin, D, H, W), dtype=torch.float32, device="cuda")
+    scratch = torch.empty(cin * cout * 27, dtype=torch.bfloat16, device="cuda")
+    k.conv_grad_input(dev(g, torch.float32), cout, dev(w.ravel(), torch.bfloat16), out, cin, dims, scratch)
+    assert rel(out.cpu().numpy(), U.conv3d_grad_input(g, w)) < 2e-6
+
+
+def test_conv_grad_weight(k):
+    rng = np.random.default_rng(8)
+    cin, cout, dims = 10, 9, (36, 10, 7)
+    W, H, D = dims
+    g = rng.standard_normal((cout, D, H, W)).astype(np.float32)
+    x = bf16(rng.standard_normal((cin, D, H, W)))
+    gw = torch.zeros(cout * cin * 27, dtype=torch.float32, device="cuda")
+    gb = torch.zeros(cout, dtype=torch.float32, device="cuda")
+    k.conv_grad_weight(dev(g, torch.float32), cout, dev(x, torch.bfloat16), cin, dims, gw, gb)
+    rw, rb = U.conv3d_grad_weight(g, x)
+    assert rel(gw.cpu().numpy().reshape(cout, cin, 27), rw) < 1e-5
+    assert rel(gb.cpu().numpy(), rb) < 1e-5
+
+
+def test_pool_upsample_and_loss(k):
+    rng = np.random.default_rng(9)
+    c, dims = 3, (8, 6, 4)
+    W, H, D = dims
+    x = rng.standard_normal((c, D, H, W)).astype(np.float32)
+    p = torch.empty((c, D // 2, H // 2, W // 2), dtype=torch.float32, device="cuda")
+    k.pool(dev(x, torch.float32), p, c, dims)
+    assert rel(p.cpu().numpy(), U.avgpool2(x)) < 1e-6
+    u = torch.empty((c, D, H, W), dtype=torch.float32, device="cuda")
+    k.up(p, u, c, dims)
+    assert rel(u.cpu().numpy(), U.upsample2(p.cpu().numpy())) < 1e-7
+    # gradients: adjoints of the linear maps
+    go = rng.standard_normal((c, D // 2, H // 2, W // 2)).astype(np.float32)
+    gi = torch.full((c, D, H, W), 1.0, dtype=torch.float32, device="cuda")
+    k.pool_grad(dev(go, torch.float32), gi, c, dims, True)
+    assert rel(gi.cpu().numpy(), 1.0 + U.upsample2(go) / 8.0) < 1e-6
+    gu = torch.empty((c, D // 2, H // 2, W // 2), dtype=torch.float32, device="cuda")
+    k.up_grad(dev(x, torch.float32), gu, c, dims)
+    assert rel(gu.cpu().numpy(), 8.0 * U.avgpool2(x)) < 1e-6
+    y, t = rng.standard_normal(1000).astype(np.float32), rng.standard_normal(1000).astype(np.float32)
+    g = torch.empty(1000, dtype=torch.float32, device="cuda")
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    k.mse(dev(y, torch.float32), dev(t, torch.float32), g, loss)
+    rl, rg = U.mse(y, t)
+    assert abs(loss.item() - rl) < 1e-5 * rl and rel(g.cpu().numpy(), rg) < 1e-6
+
+
+def test_network_gradient_matches_reference(k):
+    """Whole-network weight gradients against unet_ref.Network (float64, with the
+    activations rounded to bf16 where the kernels store them)."""
+    from ogl_beamforming_cuda_gb300.learned import UNet
+    rng = np.random.default_rng(10)
+    dims = (16, 8, 8)
+    W, H, D = dims
+    net = UNet(seed=3, kernels=k)
+    x = bf16(rng.standard_normal((2, D, H, W)))
+    t = rng.standard_normal((2, D, H, W)).astype(np.float32)
+    y = net.forward(dev(x, torch.bfloat16), dev(x, torch.float32), dims)
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    gy = torch.empty_like(y)
+    k.mse(y, dev(t, torch.float32), gy, loss)
+    net.backward(gy)
+    ref = U.Network({n: (bf16(L["w16"].float().cpu().numpy()).reshape(L["cout"], L["cin"], 27),
+                         L["b"].cpu().numpy().astype(np.float64)) for n, L in net.p.items()}, round_bf16=bf16)
+    ry = ref.forward(x)
+    assert rel(y.cpu().numpy(), ry) < 2e-3
+    rl, rgy = U.mse(ry, t)
+    grads = ref.backward(rgy)
+    # BF16 activations make single entries differ where a ReLU input sits at a
+    # rounding boundary; the gradients as a whole agree to a few 1e-3
+    for n, L in net.p.items():
+        gw = L["gw"].cpu().numpy().reshape(L["cout"], L["cin"], 27)
+        assert rel_l2(gw, grads[n][0]) < 1e-2, n
+        assert rel_l2(L["gb"].cpu().numpy(), grads[n][1]) < 1e-2, n
+
+
+def test_training_improves_on_subsampled_das():
+    """Pairs from the plain pipeline (subsampled and full-aperture DAS of seeded
+    phantoms); after a short training the network is closer to the full-aperture
+    volume than its input on held-out phantoms."""
+    from ogl_beamforming_cuda_gb300 import learned as Lm
+    torch.cuda.set_device(0)
+    k = Lm.Kernels()
+    X, Y, dims = Lm.make_dataset(48, 1000, points=(32, 32, 64), max_speckle=20000, kernels=k)
+    Xt, Yt, _ = Lm.make_dataset(8, 900000, points=(32, 32, 64), max_speckle=20000, kernels=k)
+    net, losses = Lm.train(X, Y, 600, crop=(32, 32, 32), lr=1e-3, log_every=100, kernels=k)
+    base, learned = Lm.evaluate(net, Xt, Yt, dims, kernels=k)
+    gain = float(np.mean(base - learned))
+    print(f"held-out NRMSE vs full aperture: subsampled {base.mean():.1f} dB, network {learned.mean():.1f} dB, "
+          f"gain {gain:.1f} dB")
+    assert gain > 0.5
+    assert np.all(np.isfinite(learned))
