@@ -55,9 +55,12 @@ def parse():
                     help="only push this many copies of one device-resident frame through the pipeline "
                          "(for a profiler), print per-stage ms and exit")
     ap.add_argument("--points", default=",".join(map(str, POINTS)), help="voxel grid for --profile-frames")
-    ap.add_argument("--variant", default="plain", choices=["plain", "precision", "batched"],
+    ap.add_argument("--variant", default="plain", choices=["plain", "precision", "batched", "learned"],
                     help="plain: the 3D pipeline (default, the headline line); precision: the FP16/BF16 front end "
-                         "on the 4096-sample plane; batched: 32 mixed acquisitions in one call")
+                         "on the 4096-sample plane; batched: 32 mixed acquisitions in one call; learned: every-4th-"
+                         "channel DAS + U-Net against full-aperture DAS")
+    ap.add_argument("--train-pairs", type=int, default=2000)
+    ap.add_argument("--train-steps", type=int, default=4000)
     return ap.parse_args()
 
 
@@ -493,6 +496,87 @@ def run_batched(args, peaks):
     return 0
 
 
+def run_learned(args, peaks):
+    """Learned variant on 128 x 128 x 256 volumes of the 128 + 128 HERCULES
+    acquisition (2048 samples, linear DAS): trains the U-Net on pairs the plain
+    pipeline makes from seeded phantoms, measures held-out NRMSE against
+    full-aperture DAS, and volumes/s of the learned path (every-4th-channel DAS +
+    U-Net) against the plain pipeline. The learned path is only used where its
+    held-out residual is at most -40 dB; otherwise the fallback (full DAS) runs."""
+    import torch
+    from ogl_beamforming_cuda_gb300 import learned as Lm
+    torch.cuda.set_device(0)
+    k = Lm.Kernels()
+    t0 = time.perf_counter()
+    X, Y, dims = Lm.make_dataset(args.train_pairs, 1000, kernels=k)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    Xt, Yt, _ = Lm.make_dataset(16, 900000, kernels=k)
+    t0 = time.perf_counter()
+    net, losses = Lm.train(X, Y, args.train_steps, crop=(64, 64, 64), lr=1e-3, log_every=250, kernels=k)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del X, Y
+    base, learned = Lm.evaluate(net, Xt, Yt, dims, kernels=k)
+
+    # speed: plain pipeline vs subsampled DAS + U-Net, one 128 x 128 x 256 frame each
+    bp = Lm.learned_parameters()
+    pm = Lm.PairMaker(bp, k)
+    pos, amp = Lm.phantom(424242)
+    raw = Lm.synth_rf(bp, pos, amp, 424242, k)
+    stream = torch.cuda.ExternalStream(pm.bf.lib.beamformer_gb300_get_stream())
+    W, H, D = dims
+    x16 = torch.empty((2, D, H, W), dtype=torch.bfloat16, device="cuda")
+    x32 = torch.empty((2, D, H, W), dtype=torch.float32, device="cuda")
+
+    def plain():
+        pm.das(raw, 1)
+
+    def learned_path():
+        sub = pm.das(raw, Lm.RX_STEP)
+        k.convert(sub, x32, float(Lm.RX_STEP))
+        k.convert(x32, x16)
+        net.forward(x16, x32, dims)
+    reps = max(args.steps, 3)
+    for f in (plain, learned_path):
+        f()
+    torch.cuda.synchronize()
+    h0 = time.perf_counter()
+    for _ in range(reps):
+        plain()
+    torch.cuda.synchronize()
+    ms_plain = (time.perf_counter() - h0) / reps * 1e3
+    h0 = time.perf_counter()
+    for _ in range(reps):
+        learned_path()
+    torch.cuda.synchronize()
+    ms_learned = (time.perf_counter() - h0) / reps * 1e3
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        net.forward(x16, x32, dims)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_net = e0.elapsed_time(e1) / reps
+    pm.bf.lib.beamformer_gb300_set_receive_subsampling(1)
+    fallback = bool(np.max(learned) > -40.0)
+    print(json.dumps({
+        "metric": "volumes/s of the learned path (every-4th-channel DAS + U-Net) vs full-aperture DAS",
+        "variant": "learned", "value": 1e3 / (ms_plain if fallback else ms_learned), "unit": "volumes/s",
+        "n_gpus": 1, "steps": reps, "warmup": 1, "higher_is_better": True, "dtype": "bf16 storage, f32 accumulate",
+        "data": "synthetic (seeded phantoms: points, speckle regions, 1-5 mm cysts)",
+        "config": {"workload": "128x128x256 voxels, HERCULES 128 tx x 128 rx, 2048 samples, linear DAS; U-Net "
+                               "3 levels 16/32/64, 3x3x3", "train_pairs": args.train_pairs,
+                   "train_steps": args.train_steps, "crop": [64, 64, 64], "held_out": 16},
+        "held_out_nrmse_db": {"subsampled_das": [float(v) for v in base], "network": [float(v) for v in learned],
+                              "mean_gain_db": float(np.mean(base - learned))},
+        "fallback_to_full_das": fallback,
+        "ms_per_volume": {"plain_full_das": ms_plain, "learned_path": ms_learned, "unet_forward": ms_net},
+        "learned_speedup_if_used": ms_plain / ms_learned,
+        "training": {"data_s": t_data, "train_s": t_train, "loss": losses}}))
+    return 0
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -505,6 +589,8 @@ def main():
         return run_precision(args, peaks)
     if args.variant == "batched":
         return run_batched(args, peaks)
+    if args.variant == "learned":
+        return run_learned(args, peaks)
 
     if args.impl == "reference":
         if rank != 0:
