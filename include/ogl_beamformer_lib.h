@@ -346,6 +346,17 @@ LIB_FN uint32_t beamformer_gb300_set_filter_precision(int32_t precision);
  * with UNSUPPORTED while step > 1. Takes effect at the next compute. */
 LIB_FN uint32_t beamformer_gb300_set_receive_subsampling(int32_t step);
 
+/* Serve the reference's shared-memory protocol (the `ogl` server side of
+ * helpers/ogl_beamformer_lib.c: region "/ogl_beamformer_shared_memory", version
+ * BEAMFORMER_SHARED_MEMORY_VERSION, beamformer.c:842-1111, 1230-1276) in the
+ * calling thread, computing with this library, so unmodified clients of the
+ * reference's client library beamform on this GPU. Runs until
+ * beamformer_gb300_serve_stop() or, with idle_exit_ms >= 0, until that long
+ * without work; returns 0, or -1 if the region cannot be created. No counterpart
+ * in the reference's client library; the ogl_beamformer_server executable wraps it. */
+LIB_FN int32_t beamformer_gb300_serve(int32_t idle_exit_ms);
+LIB_FN void    beamformer_gb300_serve_stop(void);
+
 /* Beamform `count` acquisitions in one go (the batched variant; no counterpart
  * in the reference, which beamforms one acquisition per compute). Acquisition i
  * has its own parameters[i] (transmit and sample counts, output grid, DAS mode),

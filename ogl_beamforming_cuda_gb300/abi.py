@@ -101,6 +101,8 @@ SIGNATURES = [
     ("beamformer_gb300_set_interpolation", u32, [i32]),
     ("beamformer_gb300_set_filter_precision", u32, [i32]),
     ("beamformer_gb300_set_receive_subsampling", u32, [i32]),
+    ("beamformer_gb300_serve", i32, [i32]),
+    ("beamformer_gb300_serve_stop", None, []),
     ("beamformer_gb300_beamform_batch", u32, [P(BeamformerParameters), u32, P(vp), P(ctypes.c_uint64), P(vp), i32]),
     ("beamformer_gb300_batch_tuning", u32, [P(i32), P(i32), P(f32), i32, P(i32)]),
     ("beamformer_gb300_das_no_alloc", u32, [P(BeamformerParameters), P(f32), P(ctypes.c_int16), vp, ctypes.c_uint64,

@@ -16,13 +16,14 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libogl_beamformer_lib.so")
+SERVER = os.path.join(LIBDIR, "ogl_beamformer_server")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 INC = [f"-I{os.path.join(ROOT, 'include')}", f"-I{CSRC}"]
 
 CU = ["bf_decode.cu", "bf_filter.cu", "bf_fir_tc.cu", "bf_das.cu", "bf_das_hercules.cu", "bf_das_batch.cu", "bf_reduce.cu", "bf_unet.cu"]
-CPP = ["bf_host.cpp", "bf_library.cpp"]
+CPP = ["bf_host.cpp", "bf_library.cpp", "bf_server.cpp"]
 HEADERS = ["bf_kernels.h", "bf_host.h", "bf_das_math.cuh", "bf_das_generic.cuh", "bf_das_hercules.cuh"]
 
 
@@ -68,6 +69,13 @@ def build(verbose=False, ptxas_info=False):
         _run([NVCC] + ARCH + ["-shared", "-cudart", "shared", "-o", tmp] + objs +
              ["-Xlinker", f"-rpath={CUDA}/lib64"])
         os.replace(tmp, LIB)
+    # the shared-memory server: a small executable on top of the library
+    srv_src = os.path.join(CSRC, "bf_server_main.cpp")
+    if not os.path.exists(SERVER) or os.path.getmtime(SERVER) < max(os.path.getmtime(srv_src), os.path.getmtime(LIB)):
+        tmp = SERVER + ".tmp"
+        _run(["g++", "-O2", "-std=c++17", "-Wall", srv_src, "-o", tmp] + INC +
+             [f"-L{LIBDIR}", "-logl_beamformer_lib", "-Wl,-rpath,$ORIGIN", "-lpthread"])
+        os.replace(tmp, SERVER)
     text = "".join(out)
     if verbose and text:
         print(text)

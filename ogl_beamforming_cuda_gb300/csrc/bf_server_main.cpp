@@ -1,0 +1,29 @@
+/*
+ * bf_server_main.cpp -- ogl_beamformer_server: serves the reference's
+ * shared-memory client protocol ("/ogl_beamformer_shared_memory", version 11)
+ * on this library until SIGINT or SIGTERM.
+ *
+ * Usage: ogl_beamformer_server [--idle-exit-ms N]   (exit after N ms without work)
+ */
+#include "ogl_beamformer_lib.h"
+
+#include <csignal>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+static void on_signal(int) { beamformer_gb300_serve_stop(); }
+
+int main(int argc, char **argv)
+{
+	int32_t idle = -1;
+	for (int i = 1; i < argc; i++)
+		if (!std::strcmp(argv[i], "--idle-exit-ms") && i + 1 < argc) idle = std::atoi(argv[++i]);
+	std::signal(SIGINT, on_signal);
+	std::signal(SIGTERM, on_signal);
+	std::fprintf(stderr, "ogl_beamformer_server: serving /ogl_beamformer_shared_memory (version %u)\n",
+	             BEAMFORMER_SHARED_MEMORY_VERSION);
+	const int32_t r = beamformer_gb300_serve(idle);
+	beamformer_gb300_shutdown();
+	return r == 0 ? 0 : 1;
+}

@@ -45,7 +45,22 @@ class Plan(ctypes.Structure):
                 ("decode", DecodeUBO), ("demod", FilterUBO), ("filter", FilterUBO), ("das", BeamformerParameters)]
 
 
+SHM_CLIENT = os.path.join(BUILD, "libshm_client.so")
+
+
+def build_shm_client(force=False):
+    """oracle/shm_client.c: the restated client side of the shared-memory protocol."""
+    src = os.path.join(HERE, "shm_client.c")
+    if not force and os.path.exists(SHM_CLIENT) and os.path.getmtime(SHM_CLIENT) >= os.path.getmtime(src):
+        return SHM_CLIENT
+    os.makedirs(BUILD, exist_ok=True)
+    subprocess.check_call(["gcc", "-std=gnu11", "-O2", "-fPIC", "-shared", "-Wall", src, "-o", SHM_CLIENT + ".tmp", "-lrt"])
+    os.replace(SHM_CLIENT + ".tmp", SHM_CLIENT)
+    return SHM_CLIENT
+
+
 def build(force=False):
+    build_shm_client(force)
     src = [os.path.join(HERE, "bf_oracle.c")]
     deps = src + [os.path.join(HERE, "bf_oracle_das.inc"), os.path.join(HERE, "bf_oracle.h")]
     if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
