@@ -17,6 +17,9 @@ is git-ignored.
                     declarations (`layout(...) buffer/uniform` lines) are
                     rewritten into C++ declarations; function bodies compile as
                     written. ref_shader_driver.cpp runs their dispatch grids.
+  zemp_probe        the zemp_bp_v1 typedef of tests/throughput.c (the captured-
+                    dataset parameter block), cut out by name and compiled into
+                    a program printing its size and field offsets.
 
 Usage: python oracle/build_ref.py [--reference PATH]. Exits 0 and builds nothing
 when the reference checkout is absent.
@@ -169,6 +172,22 @@ def build(ref):
     cc = ["gcc", "-std=c11", "-O3", "-funsafe-math-optimizations", "-fno-math-errno", "-fPIC", "-shared", "-w",
           f"-I{ref}", f"-I{OUT}"]
     run(cc + [os.path.join(HERE, "ref_math_wrap.c"), "-o", os.path.join(OUT, "libref_math.so"), "-lm"])
+    # layout of the reference's dataset header (zemp_bp_v1, tests/throughput.c): the
+    # typedef is cut from the file and compiled into a probe printing size and offsets
+    tp = open(os.path.join(ref, "tests", "throughput.c")).read()
+    m = re.search(r"#define ZEMP_BP_MAGIC.*?\n(typedef struct \{.*?\} zemp_bp_v1;)", tp, re.S)
+    if m:
+        fields = re.findall(r"^\s*\w+\s+(\w+)(?:\[\d+\])?;", m.group(1), re.M)
+        probe = os.path.join(OUT, "zemp_probe.c")
+        with open(probe, "w") as f:
+            f.write("/* generated by oracle/build_ref.py from the reference's tests/throughput.c; do not commit */\n"
+                    "#include <stdint.h>\n#include <stdio.h>\n#include <stddef.h>\n"
+                    "typedef uint64_t u64; typedef uint32_t u32; typedef uint16_t u16; typedef int16_t i16;\n"
+                    "typedef int32_t i32; typedef float f32;\n" + m.group(1) + "\n"
+                    "int main(void) {\n\tprintf(\"sizeof %zu\\n\", sizeof(zemp_bp_v1));\n" +
+                    "".join(f"\tprintf(\"{n} %zu\\n\", offsetof(zemp_bp_v1, {n}));\n" for n in fields) +
+                    "\treturn 0;\n}\n")
+        run(["gcc", "-std=c11", probe, "-o", os.path.join(OUT, "zemp_probe")])
     run(cc + [os.path.join(ref, "helpers", "ogl_beamformer_lib.c"), "-o", os.path.join(OUT, "libref_client.so"),
               "-lm"])
 
