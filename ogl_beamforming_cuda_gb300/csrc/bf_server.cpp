@@ -345,6 +345,12 @@ __attribute__((visibility("default"))) int32_t beamformer_gb300_serve(int32_t id
 	std::memset(base, 0, sizeof(SharedMemory));
 	s.sm->version = BEAMFORMER_SHARED_MEMORY_VERSION;
 	beamformer_set_global_timeout(-1);
+	/* the computing tables start as the fresh region holds them (zero), whatever
+	 * an earlier in-process user of the library left there: a client that never
+	 * uploads a table sees the same state on every start */
+	beamformer_push_channel_mapping(s.sm->channel_mapping, 256);
+	beamformer_push_focal_vectors(&s.sm->focal_vectors[0][0], 256);
+	beamformer_push_sparse_elements(s.sm->sparse_elements, 256);
 
 	auto last = std::chrono::steady_clock::now();
 	while (!g_stop) {
