@@ -22,9 +22,18 @@
  *   - The transmit-0 term (weighted by 1/sqrt(T)) is peeled off the loop.
  *   - The apodization cos^2(sqrt(w)) is one degree-6 polynomial in w (six FMAs,
  *     absolute error 1.9e-7) instead of the squared eighth-order cosine series.
- *   - The phase reduction drops the third Cody-Waite constant: with the
- *     two-constant split of 2 pi (6.28125 exact in 8 bits, the rest rounded to
- *     float) the reduced angle is off by at most |k| * 1.1e-11 rad, k < 2^15.
+ *   - Demodulated data: the phase exp(i 2 pi fc t) of a term at sample index
+ *     j + f (t = (j + f) / fs) splits into exp(i theta (j + 1/2)), stored in the
+ *     table segment of sample j, and exp(i theta (f - 1/2)), theta = 2 pi fc / fs:
+ *     one FMA and the fast sine and cosine of an angle in [-pi, pi] (|theta| <=
+ *     2 pi, which covers fc = fs / 4 of the raw data at decimation 2).
+ *     This replaces the reference's time division, angle product and range
+ *     reduction per term, and is closer to the exact phase than the float angle
+ *     of the reference (whose rounding, up to half an ulp of angles of ~10^3 rad,
+ *     is the difference). Without the table (nearest) or for larger theta the
+ *     term computes the reference's angle, reduced with the two-constant split of
+ *     2 pi (6.28125 exact in 8 bits, the rest rounded to float; off by at most
+ *     |k| * 1.1e-11 rad, k < 2^15).
  *
  * Sample indices stay bit-equal to the reference's: the delay chain is the same
  * sequence of round-to-nearest operations as das_kernel's.
@@ -41,17 +50,31 @@ namespace bf {
  * T2 = (s[n+2] - s[n]) / 2 the segment is a0 + a1 f + a2 f^2 + a3 f^3 with
  * a0 = P1, a1 = T1, a2 = 3 (P2 - P1) - 2 T1 - T2, a3 = 2 (P1 - P2) + T1 + T2;
  * stored as float4 (a0, a1) and float4 (a2, a3), complex pairs.
- * Linear: float4 (s[n], s[n+1] - s[n]). */
-template <int INTERP>
+ * Linear: float4 (s[n], s[n+1] - s[n]).
+ * ROT: every coefficient of the segment starting at sample j = n mod S of its row
+ * is multiplied by exp(i theta (j + 1/2)), the demodulation phase at the middle of
+ * the segment, from its turns (j * rot_step + rot_half) / 2^32 (0.32 fixed point:
+ * the product wraps exactly; the phase error is at most (j + 1) * 2^-33 turns). */
+template <int INTERP, bool ROT>
 __global__ void __launch_bounds__(256)
-interp_table(const float2 *__restrict__ rf, int64_t entries, int64_t readable, float4 *__restrict__ out)
+interp_table(const float2 *__restrict__ rf, int64_t entries, int64_t readable, int32_t S, uint32_t rot_step,
+             uint32_t rot_half, float4 *__restrict__ out)
 {
 	const float2 zero = make_float2(0.0f, 0.0f);
 	for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < entries; n += (int64_t)gridDim.x * blockDim.x) {
 		const float2 s1 = n < readable ? rf[n] : zero;
 		const float2 s2 = n + 1 < readable ? rf[n + 1] : zero;
+		float cs = 1.0f, sn = 0.0f;
+		if (ROT) {
+			const uint32_t u = (uint32_t)(n % S) * rot_step + rot_half;
+			sincospif((float)(int32_t)u * 0x1p-31f, &sn, &cs);
+		}
+		/* (x + i y) exp(i phi) */
+		auto rot = [&](float x, float y) { return make_float2(cs * x - sn * y, sn * x + cs * y); };
 		if (INTERP == INTERP_LINEAR) {
-			out[n] = make_float4(s1.x, s1.y, s2.x - s1.x, s2.y - s1.y);
+			const float2 a0 = ROT ? rot(s1.x, s1.y) : s1;
+			const float2 a1 = ROT ? rot(s2.x - s1.x, s2.y - s1.y) : make_float2(s2.x - s1.x, s2.y - s1.y);
+			out[n] = make_float4(a0.x, a0.y, a1.x, a1.y);
 			continue;
 		}
 		const float2 s0 = n > 0 && n - 1 < readable ? rf[n - 1] : zero;
@@ -59,9 +82,17 @@ interp_table(const float2 *__restrict__ rf, int64_t entries, int64_t readable, f
 		const float t1x = 0.5f * (s2.x - s0.x), t1y = 0.5f * (s2.y - s0.y);
 		const float t2x = 0.5f * (s3.x - s1.x), t2y = 0.5f * (s3.y - s1.y);
 		const float dx = s2.x - s1.x, dy = s2.y - s1.y;
-		out[2 * n]     = make_float4(s1.x, s1.y, t1x, t1y);
-		out[2 * n + 1] = make_float4(3.0f * dx - 2.0f * t1x - t2x, 3.0f * dy - 2.0f * t1y - t2y,
-		                             t1x + t2x - 2.0f * dx, t1y + t2y - 2.0f * dy);
+		float2 a0 = s1, a1 = make_float2(t1x, t1y);
+		float2 a2 = make_float2(3.0f * dx - 2.0f * t1x - t2x, 3.0f * dy - 2.0f * t1y - t2y);
+		float2 a3 = make_float2(t1x + t2x - 2.0f * dx, t1y + t2y - 2.0f * dy);
+		if (ROT) {
+			a0 = rot(a0.x, a0.y);
+			a1 = rot(a1.x, a1.y);
+			a2 = rot(a2.x, a2.y);
+			a3 = rot(a3.x, a3.y);
+		}
+		out[2 * n]     = make_float4(a0.x, a0.y, a1.x, a1.y);
+		out[2 * n + 1] = make_float4(a2.x, a2.y, a3.x, a3.y);
 	}
 }
 
@@ -109,8 +140,14 @@ cudaError_t launch_das_table(const DasParams &p, float4 *table, cudaStream_t s)
 	if (!table) return cudaErrorInvalidValue;
 	const int64_t entries = (int64_t)p.C * p.T * p.S;
 	const int blocks = (int)((entries + 255) / 256 < 152 * 16 ? (entries + 255) / 256 : 152 * 16);
-	if (p.interp == INTERP_CUBIC) interp_table<INTERP_CUBIC><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, table);
-	else                          interp_table<INTERP_LINEAR><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, table);
+	const bool rot = p.rot_table != 0;
+	if (p.interp == INTERP_CUBIC) {
+		if (rot) interp_table<INTERP_CUBIC, true><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, p.S, p.rot_step, p.rot_half, table);
+		else     interp_table<INTERP_CUBIC, false><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, p.S, 0, 0, table);
+	} else {
+		if (rot) interp_table<INTERP_LINEAR, true><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, p.S, p.rot_step, p.rot_half, table);
+		else     interp_table<INTERP_LINEAR, false><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, p.S, 0, 0, table);
+	}
 	g_kernel_launches++;
 	return cudaGetLastError();
 }

@@ -34,8 +34,9 @@ __device__ __forceinline__ float apod_cos2_p6(float w)
 }
 
 /* The part of one (voxel, transmit t, receive r) term after the lateral distance:
- * lat2 = |lateral offset|^2 of the virtual element (r, t); row = (r * T + t) * S. */
-template <int INTERP, bool DEMOD, bool FASTMATH>
+ * lat2 = |lateral offset|^2 of the virtual element (r, t); row = (r * T + t) * S.
+ * ROT: the table is rotated (DasParams::rot_table), the term by theta (f - 1/2) only. */
+template <int INTERP, bool DEMOD, bool FASTMATH, bool ROT>
 __device__ __forceinline__ void term_tail(const DasParams &p, const float4 *__restrict__ tab, float lat2, float dz2,
                                           float ka2, float dtx, float s_lim, int row, float scale, float &ax, float &ay)
 {
@@ -49,7 +50,7 @@ __device__ __forceinline__ void term_tail(const DasParams &p, const float4 *__re
 	const bool ok = idx >= 0.0f && idx < s_lim && w < HALF_PI_SQ;
 	const float a  = ok ? apod_cos2_p6(w) * scale : 0.0f;
 	const float ic = ok ? idx : 1.0f;
-	float vx, vy;
+	float vx, vy, f = 0.0f;
 	if (INTERP == INTERP_NEAREST) {
 		const int j = row + (int)roundf(ic);
 		const int last = (int)p.rf_count - 1;
@@ -58,7 +59,7 @@ __device__ __forceinline__ void term_tail(const DasParams &p, const float4 *__re
 		vy = j > last ? 0.0f : v.y;
 	} else {
 		const int ii = (int)ic;
-		const float f = ic - (float)ii;
+		f = ic - (float)ii;
 		if (INTERP == INTERP_CUBIC) {
 			/* one 32-byte load of the segment (the table is 32-byte aligned) */
 			const float4 *cp = tab + 2 * (size_t)(unsigned)(row + ii);
@@ -74,13 +75,17 @@ __device__ __forceinline__ void term_tail(const DasParams &p, const float4 *__re
 		}
 	}
 	if (DEMOD) {
-		const float time = FASTMATH ? div_rc(ic, p.fs, p.rfs) : __fdiv_rn(ic, p.fs);
-		const float arg  = __fmul_rn(p.r360_fc, time);
-		const float k = rintf(arg * 0.159154943f);
-		float rr = fmaf(-k, 6.28125f, arg);
-		rr = fmaf(-k, 0x1.fb5444p-10f, rr);
 		float sn, cs;
-		__sincosf(rr, &sn, &cs);
+		if (ROT && INTERP != INTERP_NEAREST) {
+			__sincosf(fmaf(p.theta, f, -p.theta_half), &sn, &cs);
+		} else {
+			const float time = FASTMATH ? div_rc(ic, p.fs, p.rfs) : __fdiv_rn(ic, p.fs);
+			const float arg  = __fmul_rn(p.r360_fc, time);
+			const float k = rintf(arg * 0.159154943f);
+			float rr = fmaf(-k, 6.28125f, arg);
+			rr = fmaf(-k, 0x1.fb5444p-10f, rr);
+			__sincosf(rr, &sn, &cs);
+		}
 		const float ca = a * cs, sa = a * sn;
 		ax = fmaf(ca, vx, fmaf(-sa, vy, ax));
 		ay = fmaf(sa, vx, fmaf(ca, vy, ay));
@@ -130,7 +135,7 @@ __device__ __forceinline__ HercVoxel hercules_setup(const DasParams &p, int vx, 
  * column). The transmit interval is the widest of the voxels' (the deepest:
  * the aperture grows with depth); a voxel's terms outside its own interval weigh
  * exactly 0, so each voxel's sums equal its own loop's bit for bit. */
-template <int INTERP, bool DEMOD, bool FASTMATH, int NV>
+template <int INTERP, bool DEMOD, bool FASTMATH, bool ROT, int NV>
 __device__ __forceinline__ void hercules_column(const DasParams &p, const float4 *__restrict__ tab, const HercVoxel *v,
                                                 int u_begin, int u_end, float *sx, float *sy)
 {
@@ -157,7 +162,7 @@ __device__ __forceinline__ void hercules_column(const DasParams &p, const float4
 			const float lat2 = __fadd_rn(f2, __fmul_rn(dv, dv));
 			#pragma unroll
 			for (int k = 0; k < NV; k++)
-				term_tail<INTERP, DEMOD, FASTMATH>(p, tab, lat2, v[k].dz2, v[k].ka2, v[k].dtx, s_lim, row, p.inv_sqrt_T,
+				term_tail<INTERP, DEMOD, FASTMATH, ROT>(p, tab, lat2, v[k].dz2, v[k].ka2, v[k].dtx, s_lim, row, p.inv_sqrt_T,
 				                                   ax[k], ay[k]);
 			t_lo = 1;
 			row += p.S;
@@ -169,7 +174,7 @@ __device__ __forceinline__ void hercules_column(const DasParams &p, const float4
 			const float lat2 = __fadd_rn(f2, __fmul_rn(dv, dv));
 			#pragma unroll
 			for (int k = 0; k < NV; k++)
-				term_tail<INTERP, DEMOD, FASTMATH>(p, tab, lat2, v[k].dz2, v[k].ka2, v[k].dtx, s_lim, row, 1.0f,
+				term_tail<INTERP, DEMOD, FASTMATH, ROT>(p, tab, lat2, v[k].dz2, v[k].ka2, v[k].dtx, s_lim, row, 1.0f,
 				                                   ax[k], ay[k]);
 			tf += 1.0f;
 			row += p.S;
@@ -184,13 +189,15 @@ template <int INTERP>
 __device__ __forceinline__ void hercules_single(const DasParams &p, const float4 *__restrict__ tab, const HercVoxel &v,
                                              int u_begin, int u_end, float &sx, float &sy)
 {
-	const bool demod = p.fc > 0.0f;
+	const bool demod = p.fc > 0.0f, rot = p.rot_table != 0;
 	if (v.fast) {
-		if (demod) hercules_column<INTERP, true, true, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
-		else       hercules_column<INTERP, false, true, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		if (demod && rot) hercules_column<INTERP, true, true, true, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else if (demod)   hercules_column<INTERP, true, true, false, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else              hercules_column<INTERP, false, true, false, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
 	} else {
-		if (demod) hercules_column<INTERP, true, false, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
-		else       hercules_column<INTERP, false, false, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		if (demod && rot) hercules_column<INTERP, true, false, true, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else if (demod)   hercules_column<INTERP, true, false, false, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else              hercules_column<INTERP, false, false, false, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
 	}
 }
 
@@ -235,9 +242,10 @@ __device__ __forceinline__ void hercules_tile(const DasParams &p, const float4 *
 		fast = fast && v[k].fast;
 	}
 	if (NV > 1 && together && fast) {
-		const bool demod = p.fc > 0.0f;
-		if (demod) hercules_column<INTERP, true, true, NV>(p, tab, v, u_begin, u_end, sx, sy);
-		else       hercules_column<INTERP, false, true, NV>(p, tab, v, u_begin, u_end, sx, sy);
+		const bool demod = p.fc > 0.0f, rot = p.rot_table != 0;
+		if (demod && rot) hercules_column<INTERP, true, true, true, NV>(p, tab, v, u_begin, u_end, sx, sy);
+		else if (demod)   hercules_column<INTERP, true, true, false, NV>(p, tab, v, u_begin, u_end, sx, sy);
+		else              hercules_column<INTERP, false, true, false, NV>(p, tab, v, u_begin, u_end, sx, sy);
 	} else {
 		#pragma unroll
 		for (int k = 0; k < NV; k++)

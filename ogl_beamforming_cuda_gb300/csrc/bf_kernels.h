@@ -100,6 +100,14 @@ struct DasParams {
 	int32_t        dense_rows;   /* rf holds exactly C*T*S samples (< 2^31), S >= 4: branch-free HERCULES path */
 	int32_t        rx_step;      /* HERCULES: receive channels 0, rx_step, 2 rx_step, ... (1 = all) */
 	float          sqrt_lo, sqrt_hi;
+	/* HERCULES table interpolation with demodulation: rot_table = 1 stores the
+	 * table segment of sample s rotated by exp(i theta (s + 1/2)), its phase in
+	 * turns being (s * rot_step + rot_half) / 2^32 (0.32 fixed point of theta / 2 pi
+	 * and theta / 4 pi, modulo 1), so a term at sample index s + f rotates only by
+	 * exp(i theta (f - 1/2)); theta = r360_fc / fs (|theta| <= 2 pi) */
+	int32_t        rot_table;
+	uint32_t       rot_step, rot_half;
+	float          theta, theta_half;
 };
 
 /* Exhaustively compare x * rb + correction with IEEE x / b for every float x in

@@ -604,6 +604,27 @@ void fill_filter_params(const Plan &pl, int i, const void *src, uint64_t src_byt
 	p.taps_len = (uint32_t)g.taps[pl.slots[i] % BEAMFORMER_FILTER_SLOTS].size();
 }
 
+/* Phase rotation of the HERCULES interpolation table (DasParams::rot_table):
+ * used for table interpolation of demodulated data while the per-term angle
+ * theta (f - 1/2), f in [0, 1), stays within [-pi, pi], the range of the fast
+ * sine and cosine. */
+static uint32_t turns_q32(double turns)
+{
+	const double fr = turns - std::floor(turns);
+	return (uint32_t)((uint64_t)std::llround(fr * 4294967296.0) & 0xffffffffu);
+}
+
+void set_das_rotation(DasParams &p)
+{
+	const double theta = (double)p.r360_fc / (double)p.fs;
+	p.theta = (float)theta;
+	p.theta_half = (float)(0.5 * theta);
+	p.rot_table = p.interp != INTERP_NEAREST && p.fc > 0.0f && std::isfinite(theta) &&
+	              std::fabs(theta) <= 2.0 * M_PI * (1.0 + 1e-6);
+	p.rot_step = p.rot_table ? turns_q32(theta / (2.0 * M_PI)) : 0;
+	p.rot_half = p.rot_table ? turns_q32(theta / (4.0 * M_PI)) : 0;
+}
+
 /* DAS stage of a plan reading channel data rf (rf_bytes readable) into frame
  * (dims, voxel transform M); the outer loop is not split (groups = 1). */
 bool fill_das_params(const Plan &pl, int kind, const void *rf, uint64_t rf_bytes, float2 *frame,
@@ -665,6 +686,7 @@ bool fill_das_params(const Plan &pl, int kind, const void *rf, uint64_t rf_bytes
 	}
 	p.groups = 1;
 	p.per_group = p.loop_end;
+	set_das_rotation(p);
 	p.rx_step = g.rx_step;
 	if (p.rx_step > 1 && (p.family != DAS_HERCULES || !p.fast || p.sparse_mode)) return fail(BF_LIB_ERR_KIND_UNSUPPORTED), false;
 	return true;
