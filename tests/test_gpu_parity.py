@@ -138,6 +138,19 @@ def test_das_hercules_plane_32_channels(interp):
     check_volume(bf.frame(0)[0], ref["frame"], f"HERCULES DASFast 32x32 interp={interp}")
 
 
+@pytest.mark.parametrize("interp", (1, 2))
+@pytest.mark.parametrize("fc_scale", (0.5, 0.77, 1.0, 1.3, 2.0))
+def test_das_hercules_phase_paths(interp, fc_scale):
+    """Demodulation phase of the table path: theta = 2 pi fc / fs up to 2 pi puts
+    the integer sample's phase into the interpolation table (the bench has theta =
+    2 pi exactly); above 2 pi the term computes the reference's angle."""
+    bp = small_params(S=2048, C=16, T=16, points=(24, 2, 48), D=2)
+    bp.center_frequency *= fc_scale
+    raw = small_raw(bp, n_points=12, n_speckle=300)
+    bf, ref = run_both(bp, [SH["Decode"], SH["Demodulate"], SH["DASFast"]], raw, interpolation=interp)
+    check_volume(bf.frame(0)[0], ref["frame"], f"HERCULES phase fc x {fc_scale} interp={interp}")
+
+
 def test_das_unknown_kind_is_zero():
     bp = small_params(S=512, C=16, T=16, das="RACES")
     raw = small_raw(bp)
