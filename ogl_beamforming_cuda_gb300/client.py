@@ -56,8 +56,11 @@ class Beamformer:
         self._check(L.beamformer_push_parameters(ctypes.byref(bp)), "parameters")
         sh = (ctypes.c_int32 * len(pipeline))(*pipeline)
         self._check(L.beamformer_push_pipeline(sh, len(pipeline), data_kind), "pipeline")
-        for stage, slot in (stage_slots or {}).items():
-            L.beamformer_set_pipeline_stage_parameters(stage, slot)
+        # every pipeline position gets its filter slot (0 unless given), so no
+        # slot of an earlier configuration carries over
+        slots = stage_slots or {}
+        for stage in range(16):
+            L.beamformer_set_pipeline_stage_parameters(stage, slots.get(stage, 0))
         self._check(L.beamformer_gb300_set_interpolation(interpolation), "interpolation")
         return self
 

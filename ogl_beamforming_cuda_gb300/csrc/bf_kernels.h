@@ -1,7 +1,7 @@
 /*
  * bf_kernels.h -- launch interface between the host library (bf_library.cpp)
  * and the sm_103a kernels (bf_decode.cu, bf_filter.cu, bf_das.cu,
- * bf_reduce.cu). Plain structs passed by value to the kernels.
+ * bf_reduce.cu, bf_hilbert.cu, ...). Plain structs passed by value to the kernels.
  */
 #pragma once
 #include <cstdint>
@@ -166,6 +166,15 @@ cudaError_t launch_das_table(const DasParams &p, float4 *table, cudaStream_t s);
  * capacity in float2 partial-sum entries (groups x voxels) */
 cudaError_t launch_das_no_alloc(DasParams p, const float4 *focal4, const int16_t *sparse, cudaStream_t s);
 int64_t     das_no_alloc_capacity();
+
+/* CudaHilbert stage (bf_hilbert.cu): analytic signal of each of `rows` rows of
+ * `samples` complex values (real parts used), in -> out; samples a power of two
+ * in [2, 16384]; twiddles = samples / 2 values from analytic_twiddles, on the
+ * device */
+bool        analytic_supported(uint32_t samples);
+void        analytic_twiddles(uint32_t samples, float2 *host_out);
+cudaError_t launch_analytic(const float2 *in, float2 *out, int64_t rows, uint32_t samples, const float2 *twiddles,
+                            cudaStream_t s);
 
 /* kernel launches issued since load (all launchers count here) */
 extern uint64_t g_kernel_launches;

@@ -136,6 +136,8 @@ struct Context {
 	uint64_t     das_partial_bytes = 0;
 	float4      *das_table = nullptr;         /* HERCULES interpolation table */
 	uint64_t     das_table_bytes = 0;
+	float2      *d_hilbert_tw = nullptr;      /* CudaHilbert FFT twiddles for hilbert_n samples */
+	uint32_t     hilbert_n = 0;
 	unsigned long long *d_mismatch = nullptr;
 	struct DivCheck { float b, lo, hi; };
 	std::vector<DivCheck> div_checks;
@@ -352,8 +354,24 @@ bool prepare()
 
 	for (int i = 0; i < pl.count; i++) {
 		int k = pl.shaders[i];
-		if (k == BeamformerShaderKind_CudaHilbert || k == BeamformerShaderKind_Render3D)
-			return fail(BF_LIB_ERR_KIND_UNSUPPORTED), false;
+		if (k == BeamformerShaderKind_Render3D) return fail(BF_LIB_ERR_KIND_UNSUPPORTED), false;
+		if (k == BeamformerShaderKind_CudaHilbert) {
+			/* analytic signal by a power-of-two FFT per row */
+			const uint32_t n = pl.das.dec_data_dim[0];
+			if (!analytic_supported(n)) return fail(BF_LIB_ERR_KIND_UNSUPPORTED), false;
+			if (n != g.hilbert_n) {
+				std::vector<float2> tw(n / 2);
+				analytic_twiddles(n, tw.data());
+				cudaStreamSynchronize(g.stream);
+				cudaFree(g.d_hilbert_tw);
+				g.d_hilbert_tw = nullptr;
+				g.hilbert_n = 0;
+				if (!cuda_ok(cudaMalloc(&g.d_hilbert_tw, tw.size() * sizeof(float2)))) return false;
+				if (!cuda_ok(cudaMemcpy(g.d_hilbert_tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice)))
+					return false;
+				g.hilbert_n = n;
+			}
+		}
 		if (k == BeamformerShaderKind_Demodulate || k == BeamformerShaderKind_DemodulateFloat ||
 		    k == BeamformerShaderKind_Filter) {
 			const FilterSpec &f = g.filters[pl.slots[i] % BEAMFORMER_FILTER_SLOTS];
@@ -735,6 +753,12 @@ bool run_stage(int i, const void *src, uint64_t src_bytes, DeviceFrame &frame, b
 		FilterParams p{};
 		fill_filter_params(pl, i, src, src_bytes, g.chan[in_idx], g.chan[out_idx], g.chan_bytes, g.stage_tables[i], p);
 		err = launch_filter(p, g.stream);
+		g.last_chan = out_idx;
+	} break;
+	case BeamformerShaderKind_CudaHilbert: {
+		/* cuda_hilbert(input, output) (beamformer.c:567-570): rows in the DAS layout */
+		const int64_t rows = (int64_t)pl.das.dec_data_dim[1] * pl.das.dec_data_dim[2];
+		err = launch_analytic(g.chan[in_idx], g.chan[out_idx], rows, pl.das.dec_data_dim[0], g.d_hilbert_tw, g.stream);
 		g.last_chan = out_idx;
 	} break;
 	case BeamformerShaderKind_DAS:
@@ -1649,6 +1673,7 @@ LIB_FN void beamformer_gb300_shutdown(void)
 	cudaFree(g.d_tc_error);
 	cudaFree(g.d_mismatch);
 	cudaFree(g.d_chmap); cudaFree(g.d_sparse); cudaFree(g.d_focal);
+	cudaFree(g.d_hilbert_tw);
 	for (auto &st : g.stage_tables) { cudaFree(st.taps); cudaFree(st.phasor); }
 	cudaStreamDestroy(g.own_stream);
 	cudaStreamDestroy(g.upload_stream);

@@ -207,6 +207,26 @@ def min_max(frame, dims):
     return out
 
 
+def analytic_signal(x):
+    """Discrete analytic signal of real rows x[..., N] (float64 result): the
+    CudaHilbert stage (BeamformerShaderKind_CudaHilbert, beamformer.c:567-570;
+    the reference runs it in its external cuda_toolkit plugin, whose source it
+    does not ship, so this restates the published definition -- Marple, IEEE
+    Trans. Signal Processing 47(9), 1999: one-sided FFT spectrum, Z[0] and Z[N/2]
+    kept, Z[1 .. N/2-1] doubled, the rest zeroed, inverse FFT). Parity for this
+    stage is unpinned by the reference."""
+    x = np.asarray(x, np.float64)
+    n = x.shape[-1]
+    h = np.zeros(n)
+    h[0] = 1.0
+    if n % 2 == 0:
+        h[n // 2] = 1.0
+        h[1:n // 2] = 2.0
+    else:
+        h[1:(n + 1) // 2] = 2.0
+    return np.fft.ifft(np.fft.fft(x, axis=-1) * h, axis=-1)
+
+
 def plan(bp, shaders, slots, data_kind, filter_specs):
     sh = np.zeros(16, np.int32)
     sh[:len(shaders)] = shaders
@@ -287,6 +307,16 @@ class OraclePipeline:
                 bufs[out_idx][:] = 0
                 L.bfo_filter(ctypes.byref(ubo), kind, _ptr(src), src.nbytes, _ptr(bufs[out_idx]), bufs[out_idx].nbytes,
                              _arr(taps, f32), len(taps), _arr(self.chmap, ctypes.c_int16), p.demod_dispatch, nt)
+                last = out_idx
+            elif kind == SHADER["CudaHilbert"]:
+                # rows of S complex samples in the DAS layout [channel][transmit][sample]
+                S, rows = int(dd[0]), int(dd[1]) * int(dd[2])
+                src = bufs[in_idx][: 2 * S * rows].reshape(rows, S, 2)
+                z = analytic_signal(src[:, :, 0])
+                bufs[out_idx][:] = 0
+                out = bufs[out_idx][: 2 * S * rows].reshape(rows, S, 2)
+                out[:, :, 0] = z.real
+                out[:, :, 1] = z.imag
                 last = out_idx
             elif kind in (SHADER["DAS"], SHADER["DASFast"]):
                 rf = bufs[in_idx][: p.rf_size // 4]
