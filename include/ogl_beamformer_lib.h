@@ -294,7 +294,11 @@ LIB_FN BeamformerLiveImagingParameters *beamformer_get_live_parameters(void);
 
 /* Use RF that already lives in device memory for the next compute instead of a
  * host push: the pipeline reads `device_data` directly (no copy). The caller
- * keeps the buffer alive and unchanged until that compute has finished.
+ * keeps the buffer alive and unchanged until that compute has finished. The
+ * compute waits for the work queued on the legacy default stream before it
+ * starts (so data written there, e.g. by PyTorch's default stream, is complete);
+ * data written on another stream needs that stream set with set_stream, or a
+ * synchronisation, first.
  * Counterpart of beamformer_push_data (ogl_beamformer_lib.c:360-382) for a
  * caller whose data is already on the GPU. */
 LIB_FN uint32_t beamformer_gb300_push_data_device(const void *device_data, uint64_t size);
@@ -371,8 +375,9 @@ LIB_FN void    beamformer_gb300_serve_stop(void);
  * tiles, one for the FORCES tiles, per 64 acquisitions); on
  * the first call for a set of parameters and pointers the tile shape and grid
  * size are autotuned on the device and the whole batch is captured in a CUDA graph,
- * which later calls with the same set replay. timeout_ms as
- * beamform_data_synchronized. Fails with UNSUPPORTED for other pipelines or a
+ * which later calls with the same set replay. As for push_data_device, the
+ * batch first waits for the work queued on the legacy default stream. timeout_ms
+ * as beamform_data_synchronized. Fails with UNSUPPORTED for other pipelines or a
  * 16-bit filter precision. */
 LIB_FN uint32_t beamformer_gb300_beamform_batch(const BeamformerParameters *parameters, uint32_t count,
                                                 const void *const *rf, const uint64_t *rf_size, float *const *out,

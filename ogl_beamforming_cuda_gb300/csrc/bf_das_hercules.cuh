@@ -35,19 +35,24 @@ __device__ __forceinline__ float apod_cos2_p6(float w)
 
 /* The part of one (voxel, transmit t, receive r) term after the lateral distance:
  * lat2 = |lateral offset|^2 of the virtual element (r, t); row = (r * T + t) * S.
- * ROT: the table is rotated (DasParams::rot_table), the term by theta (f - 1/2) only. */
-template <int INTERP, bool DEMOD, bool FASTMATH, bool ROT>
+ * ROT: the table is rotated (DasParams::rot_table), the term by theta (f - 1/2) only.
+ * INR: the voxel's proof that every sample index of its terms lies in [0, s_lim)
+ * (HercVoxel::inrange): no range test; the apodization argument is clamped to the
+ * aperture edge instead of tested, so a term just outside the aperture weighs the
+ * polynomial's value at the edge (|p| < 2e-7) where the reference weighs
+ * cos(pi/2)^2 = 2e-15. */
+template <int INTERP, bool DEMOD, bool FASTMATH, bool ROT, bool INR = false>
 __device__ __forceinline__ void term_tail(const DasParams &p, const float4 *__restrict__ tab, float lat2, float dz2,
                                           float ka2, float dtx, float s_lim, int row, float scale, float &ax, float &ay)
 {
-	const float w    = ka2 * lat2;
+	const float w    = INR ? fminf(ka2 * lat2, HALF_PI_SQ) : ka2 * lat2;
 	const float x    = __fadd_rn(lat2, dz2);
 	const float drx  = FASTMATH ? sqrt_newton(x) : __fsqrt_rn(x);
 	const float d    = __fadd_rn(dtx, drx);
 	float tt = FASTMATH ? div_rc(d, p.c, p.rc) : __fdiv_rn(d, p.c);
 	tt = __fadd_rn(tt, p.toff);
 	const float idx = __fmul_rn(tt, p.fs);
-	const bool ok = idx >= 0.0f && idx < s_lim && w < HALF_PI_SQ;
+	const bool ok = INR || (idx >= 0.0f && idx < s_lim && w < HALF_PI_SQ);
 	const float a  = ok ? apod_cos2_p6(w) * scale : 0.0f;
 	const float ic = ok ? idx : 1.0f;
 	float vx, vy, f = 0.0f;
@@ -100,6 +105,7 @@ struct HercVoxel {
 	float q_fix, q_var;     /* lateral coordinates fixed by r and varied by t */
 	float dz2, dtx, ka2, lim2;
 	bool  fast;             /* every term inside the verified fast-math ranges */
+	bool  inrange;          /* every term's sample index inside [0, S - 2) (cubic) / [0, S - 1) (linear) */
 };
 
 __device__ __forceinline__ HercVoxel hercules_setup(const DasParams &p, int vx, int vy, int vz)
@@ -127,6 +133,14 @@ __device__ __forceinline__ HercVoxel hercules_setup(const DasParams &p, int vx, 
 	v.fast = p.fast_sqrt && v.dz2 >= p.sqrt_lo && xmax <= p.sqrt_hi &&
 	         fabsf(v.dtx) + sqrtf(xmax) * 1.0001f <= p.c_hi && p.c_lo <= 0x1p-100f &&
 	         p.fs_lo <= 0x1p-100f && (float)p.S <= p.fs_hi;
+	/* distance d = dtx + sqrt(lat2 + dz2) lies in [dtx + sqrt(dz2), dtx + sqrt(xmax)]
+	 * and idx = (d / c + toff) fs grows with d; the margins (1e-4 relative, 0.01
+	 * samples) cover the roundings of the term's chain and of these bounds */
+	const float dmin = v.dtx + sqrtf(v.dz2) * 0.9999f, dmax = v.dtx + sqrtf(xmax) * 1.0001f;
+	const float imin = (dmin / p.c + p.toff) * p.fs, imax = (dmax / p.c + p.toff) * p.fs;
+	const float s_lim = (float)(p.S - (p.interp == INTERP_CUBIC ? 2 : 1));
+	v.inrange = p.interp != INTERP_NEAREST && p.c > 0.0f && p.fs > 0.0f &&
+	            imin - fabsf(imin) * 1e-4f >= 0.01f && imax + fabsf(imax) * 1e-4f + 0.01f < s_lim;
 	return v;
 }
 
@@ -135,7 +149,7 @@ __device__ __forceinline__ HercVoxel hercules_setup(const DasParams &p, int vx, 
  * column). The transmit interval is the widest of the voxels' (the deepest:
  * the aperture grows with depth); a voxel's terms outside its own interval weigh
  * exactly 0, so each voxel's sums equal its own loop's bit for bit. */
-template <int INTERP, bool DEMOD, bool FASTMATH, bool ROT, int NV>
+template <int INTERP, bool DEMOD, bool FASTMATH, bool ROT, int NV, bool INR = false>
 __device__ __forceinline__ void hercules_column(const DasParams &p, const float4 *__restrict__ tab, const HercVoxel *v,
                                                 int u_begin, int u_end, float *sx, float *sy)
 {
@@ -162,7 +176,7 @@ __device__ __forceinline__ void hercules_column(const DasParams &p, const float4
 			const float lat2 = __fadd_rn(f2, __fmul_rn(dv, dv));
 			#pragma unroll
 			for (int k = 0; k < NV; k++)
-				term_tail<INTERP, DEMOD, FASTMATH, ROT>(p, tab, lat2, v[k].dz2, v[k].ka2, v[k].dtx, s_lim, row, p.inv_sqrt_T,
+				term_tail<INTERP, DEMOD, FASTMATH, ROT, INR>(p, tab, lat2, v[k].dz2, v[k].ka2, v[k].dtx, s_lim, row, p.inv_sqrt_T,
 				                                   ax[k], ay[k]);
 			t_lo = 1;
 			row += p.S;
@@ -177,7 +191,7 @@ __device__ __forceinline__ void hercules_column(const DasParams &p, const float4
 			const float lat2 = __fadd_rn(f2, __fmul_rn(dv, dv));
 			#pragma unroll
 			for (int k = 0; k < NV; k++)
-				term_tail<INTERP, DEMOD, FASTMATH, ROT>(p, tab, lat2, v[k].dz2, v[k].ka2, v[k].dtx, s_lim, row, 1.0f,
+				term_tail<INTERP, DEMOD, FASTMATH, ROT, INR>(p, tab, lat2, v[k].dz2, v[k].ka2, v[k].dtx, s_lim, row, 1.0f,
 				                                   ax[k], ay[k]);
 			tf += 1.0f;
 			row += p.S;
@@ -246,9 +260,18 @@ __device__ __forceinline__ void hercules_tile(const DasParams &p, const float4 *
 	}
 	if (NV > 1 && together && fast) {
 		const bool demod = p.fc > 0.0f, rot = p.rot_table != 0;
-		if (demod && rot) hercules_column<INTERP, true, true, true, NV>(p, tab, v, u_begin, u_end, sx, sy);
-		else if (demod)   hercules_column<INTERP, true, true, false, NV>(p, tab, v, u_begin, u_end, sx, sy);
-		else              hercules_column<INTERP, false, true, false, NV>(p, tab, v, u_begin, u_end, sx, sy);
+		bool inr = INTERP != INTERP_NEAREST;
+		#pragma unroll
+		for (int k = 0; k < NV; k++) inr = inr && v[k].inrange;
+		if (inr) {
+			if (demod && rot) hercules_column<INTERP, true, true, true, NV, true>(p, tab, v, u_begin, u_end, sx, sy);
+			else if (demod)   hercules_column<INTERP, true, true, false, NV, true>(p, tab, v, u_begin, u_end, sx, sy);
+			else              hercules_column<INTERP, false, true, false, NV, true>(p, tab, v, u_begin, u_end, sx, sy);
+		} else {
+			if (demod && rot) hercules_column<INTERP, true, true, true, NV>(p, tab, v, u_begin, u_end, sx, sy);
+			else if (demod)   hercules_column<INTERP, true, true, false, NV>(p, tab, v, u_begin, u_end, sx, sy);
+			else              hercules_column<INTERP, false, true, false, NV>(p, tab, v, u_begin, u_end, sx, sy);
+		}
 	} else {
 		#pragma unroll
 		for (int k = 0; k < NV; k++)

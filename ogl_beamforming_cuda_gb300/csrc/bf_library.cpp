@@ -92,6 +92,7 @@ struct Context {
 	uint64_t     ext_size = 0;
 	bool         use_ext = false;
 	cudaEvent_t  ext_done = nullptr, last_done = nullptr;
+	cudaEvent_t  caller_ready = nullptr;     /* recorded on the legacy default stream */
 
 	float2      *chan[2] = {};
 	uint64_t     chan_bytes = 0;         /* allocated */
@@ -199,6 +200,7 @@ bool ensure_cuda()
 		if (!cuda_ok(cudaEventCreateWithFlags(&g.compute_done[i], cudaEventDisableTiming))) return false;
 	}
 	if (!cuda_ok(cudaEventCreateWithFlags(&g.ext_done, cudaEventDisableTiming))) return false;
+	if (!cuda_ok(cudaEventCreateWithFlags(&g.caller_ready, cudaEventDisableTiming))) return false;
 	for (auto &t : g.timing)
 		for (auto &e : t.ev)
 			if (!cuda_ok(cudaEventCreate(&e))) return false;
@@ -837,6 +839,21 @@ bool run_stage(int i, const void *src, uint64_t src_bytes, DeviceFrame &frame, b
 	return cuda_ok(err);
 }
 
+/* Device-resident inputs and outputs (push_data_device, beamform_batch): the
+ * library's streams do not synchronise implicitly with the legacy default
+ * stream, so the compute first waits for the work the caller queued there before
+ * the call (the kernels or copies that wrote its input, a clear of its output).
+ * Work on other streams of the caller is ordered by set_stream. Skipped while the
+ * compute stream is being captured into a graph, where the caller orders the graph. */
+bool order_after_caller()
+{
+	cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+	if (!cuda_ok(cudaStreamIsCapturing(g.stream, &cs))) return false;
+	if (cs != cudaStreamCaptureStatusNone) return true;
+	if (!cuda_ok(cudaEventRecord(g.caller_ready, cudaStreamLegacy))) return false;
+	return cuda_ok(cudaStreamWaitEvent(g.stream, g.caller_ready, 0));
+}
+
 uint32_t compute_base()
 {
 	if (!ensure_cuda()) return 0;
@@ -850,6 +867,7 @@ uint32_t compute_base()
 	if (g.use_ext) {
 		src = g.ext_rf;
 		src_bytes = g.ext_size;
+		if (!order_after_caller()) return 0;
 	} else {
 		slot = g.latest_slot;
 		src = g.raw[slot];
@@ -1663,6 +1681,7 @@ LIB_FN void beamformer_gb300_shutdown(void)
 		cudaEventDestroy(g.compute_done[i]);
 	}
 	cudaEventDestroy(g.ext_done);
+	cudaEventDestroy(g.caller_ready);
 	for (auto &t : g.timing)
 		for (auto &e : t.ev) cudaEventDestroy(e);
 	cudaFree(g.chan[0]); cudaFree(g.chan[1]);
@@ -1712,6 +1731,7 @@ LIB_FN uint32_t beamformer_gb300_beamform_batch(const BeamformerParameters *para
 			return 0;
 		}
 	}
+	if (!order_after_caller()) return 0;
 	if (!cuda_ok(cudaGraphLaunch(gb.exec, g.stream))) return 0;
 	g_kernel_launches += gb.graph_kernels;
 	if (!cuda_ok(cudaEventRecord(g.ext_done, g.stream))) return 0;

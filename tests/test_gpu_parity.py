@@ -203,3 +203,23 @@ def test_beamform_data_synchronized_matches_oracle():
     vol = bf.beamform(raw)
     orc = oracle_for(bf, bp, [SH["Decode"], SH["Demodulate"], SH["DAS"]], kaiser=(5.65, 5e6, 25e6, 32))
     check_volume(vol, orc.compute(raw)["frame"], "beamform_data_synchronized")
+
+
+def test_device_input_waits_for_default_stream_writes():
+    """push_data_device: RF written on the legacy default stream (PyTorch's default)
+    behind a bounded delay is complete before the library's compute reads it."""
+    import torch
+    from ogl_beamforming_cuda_gb300.client import Beamformer
+    bp = small_params(S=512, C=16, T=16)
+    raw = small_raw(bp)
+    bf = Beamformer().configure(bp, [SH["Decode"], SH["Demodulate"], SH["DAS"]], kaiser=(5.65, 5e6, 25e6, 32))
+    orc = oracle_for(bf, bp, [SH["Decode"], SH["Demodulate"], SH["DAS"]], kaiser=(5.65, 5e6, 25e6, 32))
+    ref = orc.compute(raw)
+    host = torch.from_numpy(raw).pin_memory()
+    dev = torch.zeros(raw.shape, dtype=torch.int16, device="cuda")
+    torch.cuda.synchronize()
+    torch.cuda._sleep(200_000_000)              # ~0.1 s of GPU time on the default stream
+    dev.copy_(host, non_blocking=True)          # queued behind it
+    bf.push_device(dev.data_ptr(), dev.numel() * 2)
+    bf.synchronize()
+    check_volume(bf.frame(0)[0], ref["frame"], "device input behind default-stream work")
