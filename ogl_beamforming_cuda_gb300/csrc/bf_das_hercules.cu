@@ -20,8 +20,8 @@
  *     float4). A cubic term is then one 32-byte load and a Horner evaluation in the
  *     fraction instead of four 8-byte loads, four weights and eight products.
  *   - The transmit-0 term (weighted by 1/sqrt(T)) is peeled off the loop.
- *   - The apodization cos^2(sqrt(w)) is one degree-6 polynomial in w (six FMAs,
- *     absolute error 1.9e-7) instead of the squared eighth-order cosine series.
+ *   - The apodization cos^2(sqrt(w)) is one degree-5 polynomial in w (five FMAs,
+ *     absolute error 6.4e-7) instead of the squared eighth-order cosine series.
  *   - Demodulated data: the phase exp(i 2 pi fc t) of a term at sample index
  *     j + f (t = (j + f) / fs) splits into exp(i theta (j + 1/2)), stored in the
  *     table segment of sample j, and exp(i theta (f - 1/2)), theta = 2 pi fc / fs:

@@ -19,17 +19,18 @@ __device__ __forceinline__ float div_rc(float x, float b, float rb)
 	return fmaf(r, rb, q);
 }
 
-/* cos^2(sqrt(w)) on [0, (pi/2)^2] as one degree-6 polynomial in w (Chebyshev
- * interpolation at 7 nodes; maximum absolute error 1.9e-7 in FP32 Horner form,
- * against 1e-7 for the squared Taylor cosine of the general kernel): six FMAs. */
-__device__ __forceinline__ float apod_cos2_p6(float w)
+/* cos^2(sqrt(w)) on [0, (pi/2)^2] as 1 + w q(w) with q of degree 4 (a weighted
+ * least-squares fit iterated towards the minimax error; exact at w = 0, maximum
+ * absolute error 6.4e-7 in FP32 Horner form, against 1e-7 for the squared Taylor
+ * cosine of the general kernel): five FMAs. A weight enters the sum linearly, so
+ * the error is below 1e-6 of the output. */
+__device__ __forceinline__ float apod_cos2_p5(float w)
 {
-	float c = 3.5312796e-06f;
-	c = fmaf(c, w, -1.3864083e-04f);
-	c = fmaf(c, w, 3.1705345e-03f);
-	c = fmaf(c, w, -4.4440959e-02f);
-	c = fmaf(c, w, 3.3333191e-01f);
-	c = fmaf(c, w, -9.9999976e-01f);
+	float c = -1.12993468e-04f;
+	c = fmaf(c, w, 3.10126483e-03f);
+	c = fmaf(c, w, -4.43560816e-02f);
+	c = fmaf(c, w, 3.33286583e-01f);
+	c = fmaf(c, w, -9.99991953e-01f);
 	return fmaf(c, w, 1.0f);
 }
 
@@ -39,7 +40,7 @@ __device__ __forceinline__ float apod_cos2_p6(float w)
  * INR: the voxel's proof that every sample index of its terms lies in [0, s_lim)
  * (HercVoxel::inrange): no range test; the apodization argument is clamped to the
  * aperture edge instead of tested, so a term just outside the aperture weighs the
- * polynomial's value at the edge (|p| < 2e-7) where the reference weighs
+ * polynomial's value at the edge (|p| < 5e-7) where the reference weighs
  * cos(pi/2)^2 = 2e-15. */
 template <int INTERP, bool DEMOD, bool FASTMATH, bool ROT, bool INR = false>
 __device__ __forceinline__ void term_tail(const DasParams &p, const float4 *__restrict__ tab, float lat2, float dz2,
@@ -53,7 +54,7 @@ __device__ __forceinline__ void term_tail(const DasParams &p, const float4 *__re
 	tt = __fadd_rn(tt, p.toff);
 	const float idx = __fmul_rn(tt, p.fs);
 	const bool ok = INR || (idx >= 0.0f && idx < s_lim && w < HALF_PI_SQ);
-	const float a  = ok ? apod_cos2_p6(w) * scale : 0.0f;
+	const float a  = ok ? apod_cos2_p5(w) * scale : 0.0f;
 	const float ic = ok ? idx : 1.0f;
 	float vx, vy, f = 0.0f;
 	if (INTERP == INTERP_NEAREST) {
