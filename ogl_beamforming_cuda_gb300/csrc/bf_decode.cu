@@ -8,7 +8,8 @@
  * buffer in a first pass and runs an N-term dot product per output in a second.
  * Here the channel-mapped gather is fused into the load and no scratch buffer
  * exists:
- *   - decode_fwht_i16<N>: int16 RF, Sylvester order N <= 128. One thread owns one
+ *   - decode_fwht_i16<N>: int16 RF, Sylvester order N <= 32 (64 and 128:
+ *     decode_fwht_i16_split, two threads per column). One thread owns one
  *     (channel, sample) column of N transmits in registers and applies the fast
  *     Walsh-Hadamard transform (log2 N butterfly stages, N log2 N integer adds
  *     instead of N^2 multiply-adds). Integer sums are exact; the final scale by
@@ -97,6 +98,74 @@ decode_fwht_i16(DecodeParams p)
 	}
 }
 
+/* Orders N = 64, 128: two threads per (channel, sample) column, each holding N/2
+ * transmits (lanes 0-15 of a warp the first half, 16-31 the second half, of 16
+ * columns), so a thread needs half the registers and twice the warps fit per SM.
+ * The FWHT stages inside a half run in registers; the last stage pairs transmit t
+ * with t + N/2 across the two lanes through one shuffle. Integer sums: exact in
+ * any order. Loads and stores: each half-warp moves 16 consecutive samples of one
+ * transmit row. */
+template <int N>
+__global__ void __launch_bounds__(128, 6)
+decode_fwht_i16_split(DecodeParams p)
+{
+	constexpr int H = N / 2;
+	const uint32_t lane = threadIdx.x & 31, q = lane >> 4;
+	const uint32_t s = blockIdx.x * 64 + (threadIdx.x >> 5) * 16 + (lane & 15);
+	const uint32_t c = blockIdx.y;
+	const bool live = s < p.samples;
+	const uint32_t mc = p.channel_map ? (uint32_t)(int32_t)p.channel_map[c] : c;
+	const int16_t *raw = (const int16_t *)p.in;
+	const uint64_t base = (uint64_t)p.st.in_channel * mc + (uint64_t)p.st.in_sample * s +
+	                      (uint64_t)p.st.in_transmit * (q * H);
+	const bool gathered = live && s < p.in_limit;
+	int v[H];
+	#pragma unroll
+	for (int k = 0; k < H; k++) {
+		const uint64_t idx = base + (uint64_t)p.st.in_transmit * k;
+		v[k] = (gathered && idx < p.in_elems) ? (int)__ldg(raw + idx) : 0;
+	}
+	fwht<H>(v);
+	#pragma unroll
+	for (int k = 0; k < H; k++) {
+		const int other = __shfl_xor_sync(0xffffffffu, v[k], 16);
+		v[k] = q ? other - v[k] : v[k] + other;
+	}
+	if (!live) return;
+
+	const float inv_n = 1.0f / (float)N;   /* exact: N is a power of two */
+	const uint32_t t0 = q * H;
+	if (p.output == DEC_OUT_REAL_F16 || p.output == DEC_OUT_REAL_BF16) {
+		const uint64_t pair = s >> 1;
+		uint16_t *o16 = (uint16_t *)p.out;
+		#pragma unroll
+		for (int k = 0; k < H; k++) {
+			const uint64_t o = (uint64_t)p.st.out_channel * c + (uint64_t)p.st.out_transmit * (t0 + k) +
+			                   (uint64_t)p.st.out_sample * pair;
+			const float y = __fmul_rn((float)v[k], inv_n);
+			if (o < p.out_vec2)
+				o16[2 * o + (s & 1)] = p.output == DEC_OUT_REAL_F16 ? __half_as_ushort(__float2half_rn(y))
+				                                                     : __bfloat16_as_ushort(__float2bfloat16_rn(y));
+		}
+	} else if (p.output == DEC_OUT_REAL_PAIRS) {
+		const uint64_t pair = s >> 1;
+		#pragma unroll
+		for (int k = 0; k < H; k++) {
+			const uint64_t o = (uint64_t)p.st.out_channel * c + (uint64_t)p.st.out_transmit * (t0 + k) +
+			                   (uint64_t)p.st.out_sample * pair;
+			if (o < p.out_vec2) p.out[2 * o + (s & 1)] = __fmul_rn((float)v[k], inv_n);
+		}
+	} else {
+		float2 *out = (float2 *)p.out;
+		#pragma unroll
+		for (int k = 0; k < H; k++) {
+			const uint64_t o = (uint64_t)p.st.out_channel * c + (uint64_t)p.st.out_transmit * (t0 + k) +
+			                   (uint64_t)p.st.out_sample * s;
+			if (o < p.out_vec2) out[o] = make_float2(__fmul_rn((float)v[k], inv_n), 0.0f);
+		}
+	}
+}
+
 __device__ __forceinline__ float2 load_input(const DecodeParams &p, uint64_t e)
 {
 	if (e >= p.in_elems) return make_float2(0.0f, 0.0f);
@@ -160,6 +229,13 @@ cudaError_t launch_decode(const DecodeParams &p, cudaStream_t s)
 	if (p.samples == 0 || p.channels == 0 || p.transmits == 0) return cudaSuccess;
 	bool fwht_ok = p.hadamard_mode && p.first_stage && p.input == DEC_IN_I16 && p.base == 1 &&
 	               p.transmits == p.sylvester && p.transmits <= 128;
+	if (fwht_ok && (p.transmits == 64 || p.transmits == 128)) {
+		dim3 grid((p.samples + 63) / 64, p.channels), block(128);
+		if (p.transmits == 64) decode_fwht_i16_split<64><<<grid, block, 0, s>>>(p);
+		else                   decode_fwht_i16_split<128><<<grid, block, 0, s>>>(p);
+		g_kernel_launches++;
+		return cudaGetLastError();
+	}
 	if (fwht_ok) {
 		dim3 grid((p.samples + 127) / 128, p.channels), block(128);
 		switch (p.transmits) {

@@ -18,6 +18,15 @@
  * which reads every staged sample (2R-1)/R times per tap block instead of once
  * per tap. FP32 accumulation (the order differs from the reference's by
  * rounding only).
+ *
+ * fir_reg<L, D, R, DEMOD> (the float kinds, taps padded to L in {16, 32, 64, 128},
+ * decimation D in {1, 2, 4}): a block of 64 threads owns 64 * R consecutive
+ * outputs of one row. The rotated input window is staged once in shared memory,
+ * transposed so that the lanes' reads are conflict free. Each thread makes R = 8
+ * consecutive outputs in one fully unrolled pass over its (R - 1) D + L window
+ * inputs: every staged input is read once per thread, and the taps travel by
+ * value in the kernel's parameter space, so each product is one FMA with its tap
+ * from the constant bank. The other kinds and longer filters take fir_polyphase.
  */
 #include "bf_kernels.h"
 
@@ -125,9 +134,131 @@ fir_polyphase(FilterParams p, uint32_t Lp, uint32_t stride)
 	}
 }
 
+/* ---------------- register-blocked FIR (float kinds) ---------------- */
+
+constexpr int FIRR_THREADS = 64;
+constexpr int FIRR_MAX_TAPS = 128;
+struct FirTaps { float h[FIRR_MAX_TAPS]; };      /* h[0 .. L), zero beyond the filter */
+
+template <int L, int D, int R, bool DEMOD>
+__global__ void __launch_bounds__(FIRR_THREADS)
+fir_reg(FilterParams p, const __grid_constant__ FirTaps taps)
+{
+	constexpr int NB = FIRR_THREADS * R;          /* outputs per block */
+	constexpr int RD = R * D;
+	constexpr int WIN = NB * D + L;               /* inputs j in [n0 D - L, (n0 + NB) D) */
+	constexpr int S = ((WIN + RD - 1) / RD + 1) | 1;
+	__shared__ float2 w[RD * S];
+
+	const uint32_t c = blockIdx.y, t = blockIdx.z;
+	const int64_t n0 = (int64_t)blockIdx.x * NB;
+	const int64_t j0 = n0 * D - L;
+	const uint32_t in_ch = p.map_channels ? (uint32_t)(int32_t)p.channel_map[c] : c;
+	const uint64_t in_row  = (uint64_t)p.st.in_channel * in_ch + (uint64_t)p.st.in_transmit * t;
+	const uint64_t out_row = (uint64_t)p.st.out_channel * c + (uint64_t)p.st.out_transmit * t;
+
+	/* staging in groups of G inputs per thread: all loads of a group are issued
+	 * before its rotations and stores, so G input (and phasor) loads are in flight */
+	constexpr int PER = (WIN + FIRR_THREADS - 1) / FIRR_THREADS, G = 6;
+	#pragma unroll
+	for (int k0 = 0; k0 < PER; k0 += G) {
+		float2 v[G], ph[G];
+		#pragma unroll
+		for (int k = 0; k < G; k++) {
+			const int q = threadIdx.x + (k0 + k) * FIRR_THREADS;
+			const int64_t j = j0 + q;
+			const bool in_win = k0 + k < PER && q < WIN && j >= 0 && j < (int64_t)p.in_samples;
+			const uint64_t e = in_row + (uint64_t)p.st.in_sample * (uint64_t)j;
+			v[k] = in_win && e < p.in_elems ? __ldg((const float2 *)p.in + e) : make_float2(0.0f, 0.0f);
+			if (DEMOD) ph[k] = in_win ? __ldg(p.phasor + j) : make_float2(0.0f, 0.0f);
+		}
+		#pragma unroll
+		for (int k = 0; k < G; k++) {
+			const int q = threadIdx.x + (k0 + k) * FIRR_THREADS;
+			if (k0 + k >= PER || q >= WIN) break;
+			float2 x = v[k];
+			if (DEMOD) {
+				/* sqrt(2) * rotate_iq(v * (1, -1), -j) */
+				const float x0 = x.x, y0 = -x.y;
+				x = make_float2(1.41421356f * (ph[k].x * x0 + ph[k].y * y0), 1.41421356f * (ph[k].x * y0 - ph[k].y * x0));
+			}
+			w[(q % RD) * S + q / RD] = x;
+		}
+	}
+	__syncthreads();
+
+	/* output n0 + th R + r reads inputs e = th R D + r D + k, k < L, with tap h[L - 1 - k] */
+	const int th = threadIdx.x;
+	float2 acc[R];
+	#pragma unroll
+	for (int r = 0; r < R; r++) acc[r] = make_float2(0.0f, 0.0f);
+	#pragma unroll
+	for (int i = 0; i < (R - 1) * D + L; i++) {
+		const float2 x = w[(i % RD) * S + th + i / RD];
+		#pragma unroll
+		for (int r = 0; r < R; r++) {
+			const int k = i - r * D;
+			if (k >= 0 && k < L) {
+				acc[r].x = fmaf(x.x, taps.h[L - 1 - k], acc[r].x);
+				acc[r].y = fmaf(x.y, taps.h[L - 1 - k], acc[r].y);
+			}
+		}
+	}
+	#pragma unroll
+	for (int r = 0; r < R; r++) {
+		const int64_t n = n0 + (int64_t)th * R + r;
+		if (n >= (int64_t)p.out_samples) break;
+		const uint64_t o = out_row + (uint64_t)p.st.out_sample * (uint64_t)n;
+		if (o < p.out_elems) ((float2 *)p.out)[o] = acc[r];
+	}
+}
+
+template <int L, int D>
+static void launch_fir_reg(const FilterParams &p, const FirTaps &taps, cudaStream_t s)
+{
+	constexpr int R = 8;
+	const dim3 grid((p.out_samples + FIRR_THREADS * R - 1) / (FIRR_THREADS * R), p.channels, p.transmits);
+	if (p.kind == FILT_COMPLEX) fir_reg<L, D, R, false><<<grid, FIRR_THREADS, 0, s>>>(p, taps);
+	else                        fir_reg<L, D, R, true><<<grid, FIRR_THREADS, 0, s>>>(p, taps);
+}
+
+template <int D>
+static bool launch_fir_reg_d(const FilterParams &p, const FirTaps &taps, cudaStream_t s)
+{
+	const uint32_t L = p.taps_len;
+	if (L <= 16)       launch_fir_reg<16, D>(p, taps, s);
+	else if (L <= 32)  launch_fir_reg<32, D>(p, taps, s);
+	else if (L <= 64)  launch_fir_reg<64, D>(p, taps, s);
+	else if (L <= 128) launch_fir_reg<128, D>(p, taps, s);
+	else return false;
+	return true;
+}
+
+/* the register-blocked FIR for float kinds, decimation 1, 2 or 4 and up to 128
+ * taps; false where it does not apply */
+static bool try_fir_reg(const FilterParams &p, cudaStream_t s)
+{
+	if (p.kind == FILT_DEMOD_I16 || !p.host_taps || p.taps_len == 0 || p.taps_len > FIRR_MAX_TAPS) return false;
+	if (p.kind != FILT_COMPLEX && !p.phasor) return false;
+	const uint32_t D = p.decimation ? p.decimation : 1;
+	if (D != 1 && D != 2 && D != 4) return false;
+	/* taps padded at the high end to the kernel's length: h[i] = 0 for i >= taps_len
+	 * (the window then starts earlier, and the padded taps weigh the extra inputs
+	 * by zero) */
+	FirTaps taps{};
+	for (uint32_t i = 0; i < p.taps_len; i++) taps.h[i] = p.host_taps[i];
+	if (D == 1) return launch_fir_reg_d<1>(p, taps, s);
+	if (D == 2) return launch_fir_reg_d<2>(p, taps, s);
+	return launch_fir_reg_d<4>(p, taps, s);
+}
+
 cudaError_t launch_filter(const FilterParams &p, cudaStream_t s)
 {
 	if (p.out_samples == 0 || p.channels == 0 || p.transmits == 0) return cudaSuccess;
+	if (try_fir_reg(p, s)) {
+		g_kernel_launches++;
+		return cudaGetLastError();
+	}
 	const uint32_t D = p.decimation ? p.decimation : 1;
 	const uint32_t Lp = (p.taps_len + D - 1) / D;
 	const uint32_t M = FIR_NB + Lp + FIR_R;

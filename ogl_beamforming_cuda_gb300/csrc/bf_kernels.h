@@ -61,6 +61,7 @@ struct FilterParams {
 	uint32_t       taps_len;
 	uint32_t       map_channels;
 	int            kind;
+	const float   *host_taps;      /* host, h[0 .. taps_len): the launcher passes them by value */
 };
 
 /* ---------------------------------- DAS ---------------------------------- */

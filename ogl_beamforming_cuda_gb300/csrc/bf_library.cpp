@@ -622,6 +622,7 @@ void fill_filter_params(const Plan &pl, int i, const void *src, uint64_t src_byt
 	p.taps = st.taps;
 	p.phasor = st.phasor;
 	p.taps_len = (uint32_t)g.taps[pl.slots[i] % BEAMFORMER_FILTER_SLOTS].size();
+	p.host_taps = g.taps[pl.slots[i] % BEAMFORMER_FILTER_SLOTS].data();
 }
 
 /* Phase rotation of the HERCULES interpolation table (DasParams::rot_table):
