@@ -24,6 +24,8 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+
+#include <nvtx3/nvToolsExt.h>
 #include <cstdlib>
 #include <cstring>
 #include <memory>
@@ -713,6 +715,18 @@ bool fill_das_params(const Plan &pl, int kind, const void *rf, uint64_t rf_bytes
 	return true;
 }
 
+/* NVTX range names per shader kind (enum order of beamformer_parameters.h:14-41):
+ * host ranges around each stage's launches and around a whole compute, which a
+ * profiler lines up with the stage's kernels */
+const char *stage_label(int kind)
+{
+	static const char *names[BeamformerShaderKind_Count] = {
+		"CudaDecode", "CudaHilbert", "DAS", "Decode", "Filter", "Demodulate", "MinMax", "Sum",
+		"DecodeInt16Complex", "DecodeFloat", "DecodeFloatComplex", "DecodeInt16ToFloat", "DemodulateFloat",
+		"DASFast", "Render3D"};
+	return kind >= 0 && kind < BeamformerShaderKind_Count ? names[kind] : "stage";
+}
+
 bool run_stage(int i, const void *src, uint64_t src_bytes, DeviceFrame &frame, bool &did_sum, int &sum_target)
 {
 	const Plan &pl = g.plan;
@@ -892,11 +906,19 @@ uint32_t compute_base()
 	g.last_chan = -1;
 	bool did_sum = false;
 	int sum_target = -1;
+	nvtxRangePushA("beamformer compute");
 	for (int i = 0; i < g.plan.count; i++) {
-		if (!run_stage(i, src, src_bytes, frame, did_sum, sum_target)) return 0;
+		nvtxRangePushA(stage_label(g.plan.shaders[i]));
+		const bool ok = run_stage(i, src, src_bytes, frame, did_sum, sum_target);
+		nvtxRangePop();
+		if (!ok) {
+			nvtxRangePop();
+			return 0;
+		}
 		tm.shaders[i] = g.plan.shaders[i];
 		cudaEventRecord(tm.ev[i + 1], g.stream);
 	}
+	nvtxRangePop();
 	tm.active = true;
 
 	cudaEvent_t done = g.use_ext ? g.ext_done : g.compute_done[slot];

@@ -31,6 +31,61 @@ LAYERS = (("e1a", 2, 16, True), ("e1b", 16, 16, True), ("e2a", 16, 32, True), ("
           ("d1a", 48, 16, True), ("d1b", 16, 16, True), ("out", 16, 2, False))
 RX_STEP = 4
 
+# Weight file: a plain versioned little-endian binary (no pickle, readable from C):
+# 8-byte magic, u32 version, u32 layer count, then per layer in LAYERS order a
+# 16-byte NUL-padded name, u32 cin, u32 cout, f32 w[cout][cin][27], f32 b[cout].
+WEIGHTS_MAGIC = b"BFUNETW\0"
+WEIGHTS_VERSION = 1
+
+
+def save_weights(path, state):
+    """Write state {layer: (w, b)} (tensors or arrays; every layer of LAYERS)."""
+    import struct
+    with open(path, "wb") as f:
+        f.write(WEIGHTS_MAGIC + struct.pack("<II", WEIGHTS_VERSION, len(LAYERS)))
+        for name, cin, cout, _ in LAYERS:
+            w, b = state[name]
+            w = np.asarray(w.detach().cpu() if hasattr(w, "detach") else w, dtype="<f4").reshape(-1)
+            b = np.asarray(b.detach().cpu() if hasattr(b, "detach") else b, dtype="<f4").reshape(-1)
+            if w.size != cout * cin * 27 or b.size != cout:
+                raise ValueError(f"layer {name}: {w.size} weights / {b.size} biases, expected "
+                                 f"{cout * cin * 27} / {cout}")
+            f.write(name.encode().ljust(16, b"\0") + struct.pack("<II", cin, cout))
+            f.write(w.tobytes())
+            f.write(b.tobytes())
+
+
+def load_weights(path):
+    """Read a weight file into {layer: (w float32 [cout*cin*27], b float32 [cout])};
+    ValueError for another magic, version, layer table or a short file."""
+    import struct
+    raw = open(path, "rb").read()
+    if raw[:8] != WEIGHTS_MAGIC or len(raw) < 16:
+        raise ValueError(f"{path}: not a U-Net weight file")
+    version, count = struct.unpack_from("<II", raw, 8)
+    if version != WEIGHTS_VERSION or count != len(LAYERS):
+        raise ValueError(f"{path}: version {version} with {count} layers, expected version "
+                         f"{WEIGHTS_VERSION} with {len(LAYERS)}")
+    off, state = 16, {}
+    for name, cin, cout, _ in LAYERS:
+        if off + 24 > len(raw):
+            raise ValueError(f"{path}: truncated at layer {name}")
+        fname = raw[off:off + 16].rstrip(b"\0").decode()
+        fcin, fcout = struct.unpack_from("<II", raw, off + 16)
+        if (fname, fcin, fcout) != (name, cin, cout):
+            raise ValueError(f"{path}: layer {fname} ({fcin} -> {fcout}), expected {name} ({cin} -> {cout})")
+        off += 24
+        nw, nb = cout * cin * 27, cout
+        if off + 4 * (nw + nb) > len(raw):
+            raise ValueError(f"{path}: truncated at layer {name}")
+        w = np.frombuffer(raw, "<f4", nw, off).astype(np.float32)
+        b = np.frombuffer(raw, "<f4", nb, off + 4 * nw).astype(np.float32)
+        off += 4 * (nw + nb)
+        state[name] = (w, b)
+    if off != len(raw):
+        raise ValueError(f"{path}: {len(raw) - off} trailing bytes")
+    return state
+
 
 def _bind(lib):
     vp, i32, i64, f32, u32 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctypes.c_uint32
@@ -154,9 +209,15 @@ class UNet:
 
     def load(self, state):
         for n, (w, b) in state.items():
-            self.p[n]["w"].copy_(w)
-            self.p[n]["b"].copy_(b)
+            self.p[n]["w"].copy_(torch.as_tensor(w))
+            self.p[n]["b"].copy_(torch.as_tensor(b))
             self.k.convert(self.p[n]["w"], self.p[n]["w16"])
+
+    def save_file(self, path):
+        save_weights(path, self.state())
+
+    def load_file(self, path):
+        self.load(load_weights(path))
 
     def _buf(self, c, dims, dtype=torch.bfloat16):
         return torch.empty((c, dims[2], dims[1], dims[0]), dtype=dtype, device=self.device)

@@ -145,10 +145,14 @@ def test_training_improves_on_subsampled_das():
     k = Lm.Kernels()
     X, Y, dims = Lm.make_dataset(48, 1000, points=(32, 32, 64), max_speckle=20000, kernels=k)
     Xt, Yt, _ = Lm.make_dataset(8, 900000, points=(32, 32, 64), max_speckle=20000, kernels=k)
-    net, losses = Lm.train(X, Y, 600, crop=(32, 32, 32), lr=1e-3, log_every=100, kernels=k)
+    # 1500 Adam steps at 5e-4: gains of 2.9 to 4.0 dB over repeated runs (600 steps
+    # at 1e-3 ranged from 0.3 to 3 dB: the float atomics of the weight gradient make
+    # each short training take its own path)
+    net, losses = Lm.train(X, Y, 1500, crop=(32, 32, 32), lr=5e-4, log_every=100, kernels=k)
     base, learned = Lm.evaluate(net, Xt, Yt, dims, kernels=k)
     gain = float(np.mean(base - learned))
     print(f"held-out NRMSE vs full aperture: subsampled {base.mean():.1f} dB, network {learned.mean():.1f} dB, "
           f"gain {gain:.1f} dB")
     assert gain > 0.5
     assert np.all(np.isfinite(learned))
+
