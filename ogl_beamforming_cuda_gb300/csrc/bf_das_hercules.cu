@@ -114,6 +114,19 @@ int64_t das_hercules_table_entries(const DasParams &p)
 	return p.interp == INTERP_CUBIC ? 2 * n : p.interp == INTERP_LINEAR ? n : 0;
 }
 
+int64_t das_hercules_tiles(const DasParams &p)
+{
+	if (p.dims[1] >= 4) {
+		using T = HercTile<4, herc_threads<4>()>;
+		return (int64_t)((p.dims[0] + T::X - 1) / T::X) * ((p.dims[1] + T::Y - 1) / T::Y) *
+		       ((p.dims[2] + T::Z * T::NV - 1) / (T::Z * T::NV));
+	}
+	using T = HercTile<1, herc_threads<1>()>;
+	return (int64_t)((p.dims[0] + T::X - 1) / T::X) * p.dims[1] * ((p.dims[2] + T::Z * T::NV - 1) / (T::Z * T::NV));
+}
+
+int das_hercules_blocks_per_sm() { return 1024 / herc_threads<4>(); }
+
 bool das_hercules_supported(const DasParams &p)
 {
 	return p.family == DAS_HERCULES && p.fast && !p.sparse_mode && !p.coherency && p.dense_rows &&

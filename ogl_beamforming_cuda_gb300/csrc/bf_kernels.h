@@ -135,6 +135,9 @@ cudaError_t launch_das_reduce(const float2 *partial, float2 *frame, int64_t n, i
 /* HERCULES fast path (bf_das_hercules.cu): for parameters das_hercules_supported
  * accepts; `table` holds das_hercules_table_entries float4 (none for nearest) */
 bool        das_hercules_supported(const DasParams &p);
+/* blocks of one channel group of the HERCULES launch, and resident blocks per SM */
+int64_t     das_hercules_tiles(const DasParams &p);
+int         das_hercules_blocks_per_sm();
 int64_t     das_hercules_table_entries(const DasParams &p);
 cudaError_t launch_das_hercules(const DasParams &p, float4 *table, cudaStream_t s);
 cudaError_t launch_sum(float2 *out, const float2 *const *ins, int count, float prescale, const int32_t dims[3],

@@ -715,6 +715,35 @@ bool fill_das_params(const Plan &pl, int kind, const void *rf, uint64_t rf_bytes
 	return true;
 }
 
+/* Receive channels per block group of the HERCULES launch. The launch is tiles x
+ * groups blocks on SMs x blocks-per-SM slots; when the block count is not a whole
+ * number of waves the last wave leaves slots idle (a 128 x 128 x 256 volume is
+ * 13.5 waves, a 128 x 128 plane with 16 groups 1.7). The group count is chosen to
+ * minimise that idle fraction plus the cost of the partial sums (16 B written and
+ * read per voxel and group, against about one term of work per voxel per 2 B). */
+int32_t hercules_per_group(const DasParams &p)
+{
+	static int sms = 0;
+	if (!sms && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0) != cudaSuccess) sms = 152;
+	const double slots = (double)sms * das_hercules_blocks_per_sm();
+	const int64_t tiles = das_hercules_tiles(p);
+	const double terms = (double)p.T * p.loop_end / (p.rx_step > 0 ? p.rx_step : 1);
+	double best = 1e30;
+	int32_t best_per = p.loop_end;
+	for (int g = 1; g <= p.loop_end && g <= 64; g++) {
+		int32_t per = (p.loop_end + g - 1) / g;
+		per = (per + p.rx_step - 1) / p.rx_step * p.rx_step;
+		const int32_t G = (p.loop_end + per - 1) / per;
+		const double w = (double)tiles * G / slots, waves = std::ceil(w);
+		const double cost = (waves - w) / waves + (G > 1 ? G * 2.0 / (terms > 1 ? terms : 1) : 0.0);
+		if (cost < best - 1e-9) {
+			best = cost;
+			best_per = per;
+		}
+	}
+	return best_per;
+}
+
 /* NVTX range names per shader kind (enum order of beamformer_parameters.h:14-41):
  * host ranges around each stage's launches and around a whole compute, which a
  * profiler lines up with the stage's kernels */
@@ -787,7 +816,11 @@ bool run_stage(int i, const void *src, uint64_t src_bytes, DeviceFrame &frame, b
 		p.per_group = p.loop_end;
 		const int64_t nv = (int64_t)frame.dims[0] * frame.dims[1] * frame.dims[2];
 		const int64_t vblocks = (int64_t)((frame.dims[0] + 7) / 8) * frame.dims[1] * ((frame.dims[2] + 15) / 16);
-		if (p.fast && p.loop_end > 1 && vblocks < 2048) {
+		const char *generic_env = std::getenv("OGL_BF_DAS_GENERIC");
+		if (das_hercules_supported(p) && !(generic_env && generic_env[0] == '1') && p.loop_end > 1) {
+			p.per_group = hercules_per_group(p);
+			p.groups = (p.loop_end + p.per_group - 1) / p.per_group;
+		} else if (p.fast && p.loop_end > 1 && vblocks < 2048) {
 			int64_t want = (2048 + vblocks - 1) / vblocks;
 			if (want > p.loop_end) want = p.loop_end;
 			p.per_group = (int32_t)((p.loop_end + want - 1) / want);
