@@ -12,11 +12,18 @@
  *
  * MinMax (reference: shaders/min_max.glsl:9-24, beamformer.c:595-607): level l
  * holds (min over a 2x2x2 block of level l-1's .x, max of its .y), reads
- * outside level l-1 give 0, initial values (1e9, 0). One launch per level; the
- * first level carries almost all of the traffic. Texels the reference's
- * dispatch never writes are set to NaN.
+ * outside level l-1 give 0, initial values (1e9, 0). Texels the reference's
+ * dispatch never writes are set to NaN. min_max_fused builds up to four levels
+ * per launch: a block reads the 2^k x 2^k x 2^k texels of level L0 under one
+ * level-(L0 + k) texel once into shared memory (outside level L0: 0), then
+ * makes each coarser level of that subtree from the previous one on chip and
+ * writes it (a texel outside its level is kept as 0 for the next level, one
+ * outside the dispatch as NaN, as the reference's texture holds them). A
+ * 128 x 128 x 256 frame's eight levels take two launches instead of eight.
  */
 #include "bf_kernels.h"
+
+#include <algorithm>
 
 namespace bf {
 
@@ -40,26 +47,59 @@ sum_frames(float2 *out, SumInputs ins, int count, float k, int X, int Y, int Z, 
 	}
 }
 
+struct MipLevels {
+	int32_t X[16], Y[16], Z[16];      /* level dims, max(1, d >> l); l = 0 is the frame */
+	int32_t cx[16], cy[16], cz[16];   /* the reference's dispatch bounds per level */
+	int64_t off[16];                  /* texel offset of level l >= 1 in the levels array */
+};
+
+constexpr int MM_MAX_K = 4;
+constexpr int MM_SMEM = 4096 + 512 + 64 + 8 + 1;   /* texels of a depth-4 subtree */
+
 __global__ void __launch_bounds__(256)
-min_max_level(const float2 *prev, int pX, int pY, int pZ, float2 *cur, int X, int Y, int Z, int cx, int cy, int cz)
+min_max_fused(const float2 *__restrict__ src, float2 *__restrict__ levels, const __grid_constant__ MipLevels m,
+              int L0, int k)
 {
-	const int64_t n = (int64_t)X * Y * Z;
-	for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < n; o += (int64_t)gridDim.x * blockDim.x) {
-		int x = (int)(o % X), y = (int)((o / X) % Y), z = (int)(o / ((int64_t)X * Y));
-		if (!(x < cx && y < cy && z < cz)) {
-			cur[o] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
-			continue;
-		}
-		float mn = 1000000000.0f, mx = 0.0f;
-		#pragma unroll
-		for (int k = 0; k < 8; k++) {
-			int ix = 2 * x + (k & 1), iy = 2 * y + ((k >> 1) & 1), iz = 2 * z + (k >> 2);
+	__shared__ float2 t[MM_SMEM];
+	const int S = 1 << k;
+	const int pX = m.X[L0], pY = m.Y[L0], pZ = m.Z[L0];
+	float2 *prev = t;
+	/* edges are powers of two: coordinates by shifts and masks */
+	for (int q = threadIdx.x; q < S * S * S; q += blockDim.x) {
+		const int i = q & (S - 1), j = (q >> k) & (S - 1), kk = q >> (2 * k);
+		const int x = blockIdx.x * S + i, y = blockIdx.y * S + j, z = blockIdx.z * S + kk;
+		prev[q] = (x < pX && y < pY && z < pZ) ? __ldg(src + ((int64_t)z * pY + y) * pX + x) : make_float2(0.0f, 0.0f);
+	}
+	__syncthreads();
+	int edge = S;
+	for (int lev = 1; lev <= k; lev++) {
+		const int l = L0 + lev, pe = edge, le = k - lev;   /* edge = 1 << le */
+		edge >>= 1;
+		float2 *cur = prev + pe * pe * pe;
+		const int X = m.X[l], Y = m.Y[l], Z = m.Z[l];
+		for (int q = threadIdx.x; q < edge * edge * edge; q += blockDim.x) {
+			const int i = q & (edge - 1), j = (q >> le) & (edge - 1), kk = q >> (2 * le);
+			const int x = blockIdx.x * edge + i, y = blockIdx.y * edge + j, z = blockIdx.z * edge + kk;
 			float2 v = make_float2(0.0f, 0.0f);
-			if (ix < pX && iy < pY && iz < pZ) v = __ldg(prev + ((int64_t)iz * pY + iy) * pX + ix);
-			mn = fminf(mn, v.x);
-			mx = fmaxf(mx, v.y);
+			if (x < X && y < Y && z < Z) {
+				if (x < m.cx[l] && y < m.cy[l] && z < m.cz[l]) {
+					float mn = 1000000000.0f, mx = 0.0f;
+					#pragma unroll
+					for (int c = 0; c < 8; c++) {
+						const float2 w = prev[((2 * kk + (c >> 2)) * pe + 2 * j + ((c >> 1) & 1)) * pe + 2 * i + (c & 1)];
+						mn = fminf(mn, w.x);
+						mx = fmaxf(mx, w.y);
+					}
+					v = make_float2(mn, mx);
+				} else {
+					v = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+				}
+				levels[m.off[l] + ((int64_t)z * Y + y) * X + x] = v;
+			}
+			cur[q] = v;
 		}
-		cur[o] = make_float2(mn, mx);
+		__syncthreads();
+		prev = cur;
 	}
 }
 
@@ -87,21 +127,38 @@ cudaError_t launch_sum(float2 *out, const float2 *const *ins, int count, float p
 
 cudaError_t launch_min_max(const float2 *level0, const int32_t dims[3], int mips, float2 *levels, cudaStream_t s)
 {
-	const float2 *prev = level0;
-	int pX = dims[0], pY = dims[1], pZ = dims[2];
-	float2 *cur = levels;
-	for (int l = 1; l < mips; l++) {
-		unsigned w = (unsigned)dims[0] >> l, h = (unsigned)dims[1] >> l, d = (unsigned)dims[2] >> l;
-		int X = w ? (int)w : 1, Y = h ? (int)h : 1, Z = d ? (int)d : 1;
-		int64_t n = (int64_t)X * Y * Z;
-		min_max_level<<<grid_for(n), 256, 0, s>>>(prev, pX, pY, pZ, cur, X, Y, Z, 32 * orone((int)w / 32),
-		                                           orone((int)h), 32 * orone((int)d / 32));
+	if (mips <= 1) return cudaSuccess;
+	if (mips > 16) return cudaErrorInvalidValue;
+	MipLevels m{};
+	int64_t off = 0;
+	for (int l = 0; l < mips; l++) {
+		const unsigned w = (unsigned)dims[0] >> l, h = (unsigned)dims[1] >> l, d = (unsigned)dims[2] >> l;
+		m.X[l] = w ? (int)w : 1;
+		m.Y[l] = h ? (int)h : 1;
+		m.Z[l] = d ? (int)d : 1;
+		m.cx[l] = 32 * orone((int)w / 32);
+		m.cy[l] = orone((int)h);
+		m.cz[l] = 32 * orone((int)d / 32);
+		if (l >= 1) {
+			m.off[l] = off;
+			off += (int64_t)m.X[l] * m.Y[l] * m.Z[l];
+		}
+	}
+	for (int L0 = 0; L0 < mips - 1; L0 += MM_MAX_K) {
+		const int k = mips - 1 - L0 < MM_MAX_K ? mips - 1 - L0 : MM_MAX_K;
+		/* blocks: enough subtrees to cover every level written by this launch */
+		int gx = 1, gy = 1, gz = 1;
+		for (int lev = 1; lev <= k; lev++) {
+			const int sh = k - lev, l = L0 + lev;
+			gx = std::max(gx, (m.X[l] + (1 << sh) - 1) >> sh);
+			gy = std::max(gy, (m.Y[l] + (1 << sh) - 1) >> sh);
+			gz = std::max(gz, (m.Z[l] + (1 << sh) - 1) >> sh);
+		}
+		const float2 *src = L0 == 0 ? level0 : levels + m.off[L0];
+		min_max_fused<<<dim3(gx, gy, gz), 256, 0, s>>>(src, levels, m, L0, k);
 		g_kernel_launches++;
-		cudaError_t e = cudaGetLastError();
+		const cudaError_t e = cudaGetLastError();
 		if (e != cudaSuccess) return e;
-		prev = cur;
-		pX = X; pY = Y; pZ = Z;
-		cur += n;
 	}
 	return cudaSuccess;
 }

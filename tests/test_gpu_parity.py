@@ -223,3 +223,24 @@ def test_device_input_waits_for_default_stream_writes():
     bf.push_device(dev.data_ptr(), dev.numel() * 2)
     bf.synchronize()
     check_volume(bf.frame(0)[0], ref["frame"], "device input behind default-stream work")
+
+
+@pytest.mark.parametrize("dims", [(64, 2, 64), (17, 1, 40), (100, 3, 70), (128, 1, 128), (33, 65, 7), (1, 1, 1),
+                                  (256, 4, 96)])
+def test_min_max_pyramid_shapes(dims):
+    """Every mip level bit-exact against the oracle for sizes that are not powers
+    of two, planes, single texels and frames whose dispatch leaves NaN regions."""
+    from ogl_beamforming_cuda_gb300.client import Beamformer
+    from oracle import bf_oracle as O
+    bp = small_params(S=256, C=8, T=8, points=dims)
+    pipe = [SH["Decode"], SH["Demodulate"], SH["DAS"], SH["MinMax"]]
+    bf = Beamformer().configure(bp, pipe, kaiser=(5.65, 5e6, 25e6, 16))
+    bf.push(small_raw(bp))
+    bf.synchronize()
+    das, _ = bf.frame(0)
+    levels = O.min_max(das, dims)
+    off = 0
+    for lvl in range(1, O.frame_mips(dims)):
+        got, d = bf.frame(0, lvl)
+        assert np.array_equal(got, levels[off:off + got.size], equal_nan=True), f"mip {lvl} of {dims}"
+        off += got.size
