@@ -245,8 +245,6 @@ cudaError_t launch_decode(const DecodeParams &p, cudaStream_t s)
 		case 8:   decode_fwht_i16<8><<<grid, block, 0, s>>>(p); break;
 		case 16:  decode_fwht_i16<16><<<grid, block, 0, s>>>(p); break;
 		case 32:  decode_fwht_i16<32><<<grid, block, 0, s>>>(p); break;
-		case 64:  decode_fwht_i16<64><<<grid, block, 0, s>>>(p); break;
-		case 128: decode_fwht_i16<128><<<grid, block, 0, s>>>(p); break;
 		default:  fwht_ok = false; break;
 		}
 		if (fwht_ok) {
