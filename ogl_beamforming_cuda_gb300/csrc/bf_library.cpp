@@ -723,8 +723,10 @@ bool fill_das_params(const Plan &pl, int kind, const void *rf, uint64_t rf_bytes
  * read per voxel and group, against about one term of work per voxel per 2 B). */
 int32_t hercules_per_group(const DasParams &p)
 {
-	static int sms = 0;
-	if (!sms && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0) != cudaSuccess) sms = 152;
+	int dev = 0, sms = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+	    sms <= 0)
+		sms = 152;
 	const double slots = (double)sms * das_hercules_blocks_per_sm();
 	const int64_t tiles = das_hercules_tiles(p);
 	const double terms = (double)p.T * p.loop_end / (p.rx_step > 0 ? p.rx_step : 1);
