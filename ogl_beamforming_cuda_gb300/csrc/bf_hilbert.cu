@@ -13,12 +13,13 @@
  * zeroed; z = IFFT(Z) = conj(FFT(conj(Z))) / N.
  *
  * The row is read once from HBM into shared memory and written once; both
- * transforms stay on chip. N <= 8192: Stockham autosort FFT (natural order in
- * and out, no bit reversal; Govindaraju et al., "High performance discrete
- * Fourier transforms on graphics processors", SC 2008) in radix-8 passes and one
- * radix-4 or radix-2 pass, ping-pong between two shared buffers whose index is
- * padded by one element per 32 (the strided writes of the early passes then
- * spread over the banks). Rows shorter than 2048 samples share a CTA. N = 16384:
+ * transforms stay on chip. N <= 8192: the real-input form (two N/2-point
+ * transforms, see analytic_rows_stockham) with a Stockham autosort FFT (natural
+ * order in and out, no bit reversal; Govindaraju et al., "High performance
+ * discrete Fourier transforms on graphics processors", SC 2008) in radix-8 passes
+ * and one radix-4 or radix-2 pass, ping-pong between two shared buffers whose
+ * index is padded by one element per 32 (the strided writes of the early passes
+ * then spread over the banks). Rows shorter than 4096 samples share a CTA. N = 16384:
  * in-place radix-2 (bit-reversed load, decimation in time forward, decimation in
  * frequency inverse), 128 KB of shared memory. Twiddles w[m] = exp(-2 pi i m / N),
  * m < N / 2, come from a table the host computes in double precision.
@@ -133,10 +134,10 @@ static __device__ __forceinline__ void dft8(float2 *v)
  * length Ns become length Ns * R. */
 template <int R>
 static __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, float2 *__restrict__ dst, int E,
-                                                     int N, int Ns, const float2 *__restrict__ tw)
+                                                     int N, int Ns, const float2 *__restrict__ tw, int tw_n)
 {
 	const int per_row = N / R;
-	const int tstep = N / (Ns * R);
+	const int tstep = tw_n / (Ns * R);                 /* tw[m] = exp(-2 pi i m / tw_n) */
 	for (int g = threadIdx.x; g < E / R; g += blockDim.x) {
 		const int row = g / per_row, j = g - row * per_row;
 		const int base = row * N, k = j % Ns;
@@ -158,69 +159,109 @@ static __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ 
 	}
 }
 
-/* forward FFT of every row of buf[0]; returns the buffer holding the result */
-static __device__ float2 *stockham_fft(float2 *b0, float2 *b1, int E, int N, const float2 *__restrict__ tw)
+/* forward N-point FFT of every row of b0 (twiddles from a table for tw_n >= N
+ * points); returns the buffer holding the result */
+static __device__ float2 *stockham_fft(float2 *b0, float2 *b1, int E, int N, const float2 *__restrict__ tw, int tw_n)
 {
 	int Ns = 1;
 	while (N / Ns >= 8) {
-		stockham_pass<8>(b0, b1, E, N, Ns, tw);
+		stockham_pass<8>(b0, b1, E, N, Ns, tw, tw_n);
 		__syncthreads();
 		float2 *t = b0; b0 = b1; b1 = t;
 		Ns *= 8;
 	}
 	if (N / Ns == 4) {
-		stockham_pass<4>(b0, b1, E, N, Ns, tw);
+		stockham_pass<4>(b0, b1, E, N, Ns, tw, tw_n);
 		__syncthreads();
 		float2 *t = b0; b0 = b1; b1 = t;
 	} else if (N / Ns == 2) {
-		stockham_pass<2>(b0, b1, E, N, Ns, tw);
+		stockham_pass<2>(b0, b1, E, N, Ns, tw, tw_n);
 		__syncthreads();
 		float2 *t = b0; b0 = b1; b1 = t;
 	}
 	return b0;
 }
 
+static __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+static __device__ __forceinline__ float2 cscale(float2 a, float k) { return make_float2(a.x * k, a.y * k); }
+/* a * (-i/2): the 1/(2i) of the even/odd split */
+static __device__ __forceinline__ float2 cmhalfi(float2 a) { return make_float2(0.5f * a.y, -0.5f * a.x); }
+
+/* Real-input form (N = 2M): y[m] = x[2m] + i x[2m+1] is transformed with M points,
+ * Y = FFT_M(y). Each pair (k, M - k) of Y gives X[k] = E[k] + W^k O[k] with
+ * E[k] = (Y[k] + conj Y[M-k]) / 2, O[k] = (Y[k] - conj Y[M-k]) / (2i), W = exp(-2 pi
+ * i / N), for X[k] and X[M-k] at once. The Hilbert spectrum H[k] = -i X[k]
+ * (0 < k < M; H[0] = H[M] = 0) is Hermitian, so its real inverse h = H{x} comes
+ * from one more M-point transform of V[k] = (H[k] + conj H[M-k]) / 2 +
+ * i (H[k] - conj H[M-k]) W^-k / 2: h[2m] + i h[2m+1] = IFFT_M(V)[m]. The output is
+ * z = x + i h, whose real part is x itself. */
 __global__ void __launch_bounds__(256)
 analytic_rows_stockham(const float2 *__restrict__ in, float2 *__restrict__ out, int64_t rows, int n, int rows_per_cta,
                        const float2 *__restrict__ tw)
 {
 	extern __shared__ float2 smem[];
-	const int E = n * rows_per_cta, padded = E + (E >> 5);
+	const int m = n >> 1;
+	const int lm = 31 - __clz(m);                 /* m = 1 << lm */
+	const int E = m * rows_per_cta, padded = E + (E >> 5);
 	float2 *b0 = smem, *b1 = smem + padded;
-	const int half = n >> 1;
-	const float scale = 1.0f / (float)n;
+	const float scale = 1.0f / (float)m;
+	const int P = (m >> 1) + 1;                   /* pairs (k, m - k) per row, k = 0 .. m/2 */
 	for (int64_t row0 = (int64_t)blockIdx.x * rows_per_cta; row0 < rows; row0 += (int64_t)gridDim.x * rows_per_cta) {
-		const int64_t avail = rows - row0;
-		const int E_rows = (int)(avail < rows_per_cta ? avail : rows_per_cta) * n;
 		const float2 *src = in + row0 * n;
 		float2 *dst = out + row0 * n;
-		for (int e = threadIdx.x; e < E; e += blockDim.x)
-			b0[pad(e)] = make_float2(e < E_rows ? __ldcs(src + e).x : 0.0f, 0.0f);
-		__syncthreads();
-		float2 *f = stockham_fft(b0, b1, E, n, tw);
-		float2 *o = f == b0 ? b1 : b0;
-		/* one-sided spectrum, conjugated for the inverse transform */
+		const int64_t avail = rows - row0;
+		const int E_rows = (int)(avail < rows_per_cta ? avail : rows_per_cta) * m;
 		for (int e = threadIdx.x; e < E; e += blockDim.x) {
-			const int s = e & (n - 1);
-			const float g = (s == 0 || s == half) ? 1.0f : (s < half ? 2.0f : 0.0f);
-			const float2 z = f[pad(e)];
-			f[pad(e)] = make_float2(z.x * g, -z.y * g);
+			float2 y = make_float2(0.0f, 0.0f);
+			if (e < E_rows) {
+				const float4 v = __ldg((const float4 *)(src + 2 * (int64_t)e));   /* samples 2k and 2k + 1 */
+				y = make_float2(v.x, v.z);
+			}
+			b0[pad(e)] = y;
 		}
 		__syncthreads();
-		float2 *r = stockham_fft(f, o, E, n, tw);
+		float2 *f = stockham_fft(b0, b1, E, m, tw, n);
+		float2 *o = f == b0 ? b1 : b0;
+		for (int q = threadIdx.x; q < rows_per_cta * P; q += blockDim.x) {
+			const int r = q / P, k = q - r * P, kk = (m - k) & (m - 1);
+			const int base = r << lm;
+			const float2 Yk = f[pad(base + k)], Ykk = f[pad(base + kk)];
+			const float2 Wk = __ldg(tw + k), Wkk = __ldg(tw + kk);
+			const float2 Xk  = cadd(cscale(cadd(Yk, cconj(Ykk)), 0.5f), cmul(Wk, cmhalfi(csub(Yk, cconj(Ykk)))));
+			const float2 Xkk = cadd(cscale(cadd(Ykk, cconj(Yk)), 0.5f), cmul(Wkk, cmhalfi(csub(Ykk, cconj(Yk)))));
+			const float2 Hk  = k == 0 ? make_float2(0.0f, 0.0f) : cmi(Xk);
+			const float2 Hkk = kk == 0 ? make_float2(0.0f, 0.0f) : cmi(Xkk);
+			const float2 HMk = k == 0 ? make_float2(0.0f, 0.0f) : Hkk;      /* H[M - k] */
+			const float2 HMkk = kk == 0 ? make_float2(0.0f, 0.0f) : Hk;     /* H[M - kk] */
+			/* V = (H + conj H') / 2 + i (H - conj H') conj(W) / 2; stored conjugated for the
+			 * inverse transform done as a forward one */
+			const float2 dk = cmul(csub(Hk, cconj(HMk)), cconj(Wk));
+			const float2 Vk = cadd(cscale(cadd(Hk, cconj(HMk)), 0.5f), make_float2(-0.5f * dk.y, 0.5f * dk.x));
+			o[pad(base + k)] = cconj(Vk);
+			if (kk != k) {
+				const float2 dkk = cmul(csub(Hkk, cconj(HMkk)), cconj(Wkk));
+				const float2 Vkk = cadd(cscale(cadd(Hkk, cconj(HMkk)), 0.5f), make_float2(-0.5f * dkk.y, 0.5f * dkk.x));
+				o[pad(base + kk)] = cconj(Vkk);
+			}
+		}
+		__syncthreads();
+		float2 *res = stockham_fft(o, f, E, m, tw, n);
 		for (int e = threadIdx.x; e < E_rows; e += blockDim.x) {
-			const float2 z = r[pad(e)];
-			__stcs(dst + e, make_float2(z.x * scale, -z.y * scale));
+			const float2 v = cscale(cconj(res[pad(e)]), scale);                   /* h[2k] + i h[2k + 1] */
+			const float4 xin = __ldg((const float4 *)(src + 2 * (int64_t)e));
+			__stcs((float4 *)(dst + 2 * (int64_t)e), make_float4(xin.x, v.x, xin.z, v.y));
 		}
 		__syncthreads();
 	}
 }
 
-static int stockham_rows_per_cta(uint32_t n) { return n >= 2048 ? 1 : (int)(2048 / n); }
+/* rows of n real samples are m = n / 2 complex points on chip; rows shorter than
+ * 2048 points share a CTA */
+static int stockham_rows_per_cta(uint32_t n) { return n / 2 >= 2048 ? 1 : (int)(2048 / (n / 2)); }
 
 static size_t stockham_smem(uint32_t n)
 {
-	const size_t E = (size_t)n * stockham_rows_per_cta(n);
+	const size_t E = (size_t)(n / 2) * stockham_rows_per_cta(n);
 	return 2 * (E + (E >> 5)) * sizeof(float2);
 }
 
