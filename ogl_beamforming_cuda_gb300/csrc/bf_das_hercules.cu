@@ -26,11 +26,12 @@
  *     j + f (t = (j + f) / fs) splits into exp(i theta (j + 1/2)), stored in the
  *     table segment of sample j, and exp(i theta (f - 1/2)), theta = 2 pi fc / fs:
  *     one FMA and the fast sine and cosine of an angle in [-pi, pi] (|theta| <=
- *     2 pi, which covers fc = fs / 4 of the raw data at decimation 2).
+ *     2 pi, which covers fc = fs / 4 of the raw data at decimation 2; larger
+ *     theta, e.g. 4 pi at decimation 4, adds a two-constant reduction).
  *     This replaces the reference's time division, angle product and range
  *     reduction per term, and is closer to the exact phase than the float angle
  *     of the reference (whose rounding, up to half an ulp of angles of ~10^3 rad,
- *     is the difference). Without the table (nearest) or for larger theta the
+ *     is the difference). Without the table (nearest), or for |theta| > 256, the
  *     term computes the reference's angle, reduced with the two-constant split of
  *     2 pi (6.28125 exact in 8 bits, the rest rounded to float; off by at most
  *     |k| * 1.1e-11 rad, k < 2^15).
@@ -125,7 +126,26 @@ int64_t das_hercules_tiles(const DasParams &p)
 	return (int64_t)((p.dims[0] + T::X - 1) / T::X) * p.dims[1] * ((p.dims[2] + T::Z * T::NV - 1) / (T::Z * T::NV));
 }
 
-int das_hercules_blocks_per_sm() { return 1024 / herc_threads<4>(); }
+template <int TY>
+static int hercules_occupancy(int interp)
+{
+	int n = 0;
+	cudaError_t e;
+	switch (interp) {
+	case INTERP_CUBIC:  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, das_hercules<INTERP_CUBIC, TY>, herc_threads<TY>(), 0); break;
+	case INTERP_LINEAR: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, das_hercules<INTERP_LINEAR, TY>, herc_threads<TY>(), 0); break;
+	default:            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, das_hercules<INTERP_NEAREST, TY>, herc_threads<TY>(), 0); break;
+	}
+	return e == cudaSuccess && n > 0 ? n : 1024 / herc_threads<TY>();
+}
+
+int das_hercules_blocks_per_sm(const DasParams &p)
+{
+	static int cache[2][3] = {};
+	const int ty = p.dims[1] >= 4 ? 1 : 0, ip = p.interp >= 0 && p.interp < 3 ? p.interp : 0;
+	if (!cache[ty][ip]) cache[ty][ip] = ty ? hercules_occupancy<4>(p.interp) : hercules_occupancy<1>(p.interp);
+	return cache[ty][ip];
+}
 
 bool das_hercules_supported(const DasParams &p)
 {

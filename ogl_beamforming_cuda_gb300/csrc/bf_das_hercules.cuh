@@ -36,13 +36,14 @@ __device__ __forceinline__ float apod_cos2_p5(float w)
 
 /* The part of one (voxel, transmit t, receive r) term after the lateral distance:
  * lat2 = |lateral offset|^2 of the virtual element (r, t); row = (r * T + t) * S.
- * ROT: the table is rotated (DasParams::rot_table), the term by theta (f - 1/2) only.
+ * ROT: the table is rotated (DasParams::rot_table), the term by theta (f - 1/2)
+ * only; ROT = 2 reduces that angle to [-pi, pi] first (|theta| > 2 pi).
  * INR: the voxel's proof that every sample index of its terms lies in [0, s_lim)
  * (HercVoxel::inrange): no range test; the apodization argument is clamped to the
  * aperture edge instead of tested, so a term just outside the aperture weighs the
  * polynomial's value at the edge (|p| < 5e-7) where the reference weighs
  * cos(pi/2)^2 = 2e-15. */
-template <int INTERP, bool DEMOD, bool FASTMATH, bool ROT, bool INR = false>
+template <int INTERP, bool DEMOD, bool FASTMATH, int ROT, bool INR = false>
 __device__ __forceinline__ void term_tail(const DasParams &p, const float4 *__restrict__ tab, float lat2, float dz2,
                                           float ka2, float dtx, float s_lim, int row, float scale, float &ax, float &ay)
 {
@@ -82,8 +83,15 @@ __device__ __forceinline__ void term_tail(const DasParams &p, const float4 *__re
 	}
 	if (DEMOD) {
 		float sn, cs;
-		if (ROT && INTERP != INTERP_NEAREST) {
-			__sincosf(fmaf(p.theta, f, -p.theta_half), &sn, &cs);
+		if (ROT != 0 && INTERP != INTERP_NEAREST) {
+			float a = fmaf(p.theta, f, -p.theta_half);
+			if (ROT == 2) {
+				/* two-constant split of 2 pi: off by at most |k| * 1.1e-11 rad */
+				const float k = rintf(a * 0.159154943f);
+				a = fmaf(-k, 6.28125f, a);
+				a = fmaf(-k, 0x1.fb5444p-10f, a);
+			}
+			__sincosf(a, &sn, &cs);
 		} else {
 			const float time = FASTMATH ? div_rc(ic, p.fs, p.rfs) : __fdiv_rn(ic, p.fs);
 			const float arg  = __fmul_rn(p.r360_fc, time);
@@ -150,7 +158,7 @@ __device__ __forceinline__ HercVoxel hercules_setup(const DasParams &p, int vx, 
  * column). The transmit interval is the widest of the voxels' (the deepest:
  * the aperture grows with depth); a voxel's terms outside its own interval weigh
  * exactly 0, so each voxel's sums equal its own loop's bit for bit. */
-template <int INTERP, bool DEMOD, bool FASTMATH, bool ROT, int NV, bool INR = false>
+template <int INTERP, bool DEMOD, bool FASTMATH, int ROT, int NV, bool INR = false>
 __device__ __forceinline__ void hercules_column(const DasParams &p, const float4 *__restrict__ tab, const HercVoxel *v,
                                                 int u_begin, int u_end, float *sx, float *sy)
 {
@@ -207,15 +215,18 @@ template <int INTERP>
 __device__ __forceinline__ void hercules_single(const DasParams &p, const float4 *__restrict__ tab, const HercVoxel &v,
                                              int u_begin, int u_end, float &sx, float &sy)
 {
-	const bool demod = p.fc > 0.0f, rot = p.rot_table != 0;
+	const bool demod = p.fc > 0.0f;
+	const int rot = p.rot_table;
 	if (v.fast) {
-		if (demod && rot) hercules_column<INTERP, true, true, true, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
-		else if (demod)   hercules_column<INTERP, true, true, false, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
-		else              hercules_column<INTERP, false, true, false, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		if (demod && rot == 1)      hercules_column<INTERP, true, true, 1, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else if (demod && rot == 2) hercules_column<INTERP, true, true, 2, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else if (demod)             hercules_column<INTERP, true, true, 0, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else                        hercules_column<INTERP, false, true, 0, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
 	} else {
-		if (demod && rot) hercules_column<INTERP, true, false, true, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
-		else if (demod)   hercules_column<INTERP, true, false, false, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
-		else              hercules_column<INTERP, false, false, false, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		if (demod && rot == 1)      hercules_column<INTERP, true, false, 1, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else if (demod && rot == 2) hercules_column<INTERP, true, false, 2, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else if (demod)             hercules_column<INTERP, true, false, 0, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else                        hercules_column<INTERP, false, false, 0, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
 	}
 }
 
@@ -260,18 +271,21 @@ __device__ __forceinline__ void hercules_tile(const DasParams &p, const float4 *
 		fast = fast && v[k].fast;
 	}
 	if (NV > 1 && together && fast) {
-		const bool demod = p.fc > 0.0f, rot = p.rot_table != 0;
+		const bool demod = p.fc > 0.0f;
+		const int rot = p.rot_table;
 		bool inr = INTERP != INTERP_NEAREST;
 		#pragma unroll
 		for (int k = 0; k < NV; k++) inr = inr && v[k].inrange;
 		if (inr) {
-			if (demod && rot) hercules_column<INTERP, true, true, true, NV, true>(p, tab, v, u_begin, u_end, sx, sy);
-			else if (demod)   hercules_column<INTERP, true, true, false, NV, true>(p, tab, v, u_begin, u_end, sx, sy);
-			else              hercules_column<INTERP, false, true, false, NV, true>(p, tab, v, u_begin, u_end, sx, sy);
+			if (demod && rot == 1)      hercules_column<INTERP, true, true, 1, NV, true>(p, tab, v, u_begin, u_end, sx, sy);
+			else if (demod && rot == 2) hercules_column<INTERP, true, true, 2, NV, true>(p, tab, v, u_begin, u_end, sx, sy);
+			else if (demod)             hercules_column<INTERP, true, true, 0, NV, true>(p, tab, v, u_begin, u_end, sx, sy);
+			else                        hercules_column<INTERP, false, true, 0, NV, true>(p, tab, v, u_begin, u_end, sx, sy);
 		} else {
-			if (demod && rot) hercules_column<INTERP, true, true, true, NV>(p, tab, v, u_begin, u_end, sx, sy);
-			else if (demod)   hercules_column<INTERP, true, true, false, NV>(p, tab, v, u_begin, u_end, sx, sy);
-			else              hercules_column<INTERP, false, true, false, NV>(p, tab, v, u_begin, u_end, sx, sy);
+			if (demod && rot == 1)      hercules_column<INTERP, true, true, 1, NV>(p, tab, v, u_begin, u_end, sx, sy);
+			else if (demod && rot == 2) hercules_column<INTERP, true, true, 2, NV>(p, tab, v, u_begin, u_end, sx, sy);
+			else if (demod)             hercules_column<INTERP, true, true, 0, NV>(p, tab, v, u_begin, u_end, sx, sy);
+			else                        hercules_column<INTERP, false, true, 0, NV>(p, tab, v, u_begin, u_end, sx, sy);
 		}
 	} else {
 		#pragma unroll

@@ -105,7 +105,8 @@ struct DasParams {
 	 * table segment of sample s rotated by exp(i theta (s + 1/2)), its phase in
 	 * turns being (s * rot_step + rot_half) / 2^32 (0.32 fixed point of theta / 2 pi
 	 * and theta / 4 pi, modulo 1), so a term at sample index s + f rotates only by
-	 * exp(i theta (f - 1/2)); theta = r360_fc / fs (|theta| <= 2 pi) */
+	 * exp(i theta (f - 1/2)); theta = r360_fc / fs. rot_table = 2: that angle is
+	 * reduced to [-pi, pi] per term (|theta| > 2 pi) */
 	int32_t        rot_table;
 	uint32_t       rot_step, rot_half;
 	float          theta, theta_half;
@@ -137,7 +138,7 @@ cudaError_t launch_das_reduce(const float2 *partial, float2 *frame, int64_t n, i
 bool        das_hercules_supported(const DasParams &p);
 /* blocks of one channel group of the HERCULES launch, and resident blocks per SM */
 int64_t     das_hercules_tiles(const DasParams &p);
-int         das_hercules_blocks_per_sm();
+int         das_hercules_blocks_per_sm(const DasParams &p);
 int64_t     das_hercules_table_entries(const DasParams &p);
 cudaError_t launch_das_hercules(const DasParams &p, float4 *table, cudaStream_t s);
 cudaError_t launch_sum(float2 *out, const float2 *const *ins, int count, float prescale, const int32_t dims[3],

@@ -628,9 +628,10 @@ void fill_filter_params(const Plan &pl, int i, const void *src, uint64_t src_byt
 }
 
 /* Phase rotation of the HERCULES interpolation table (DasParams::rot_table):
- * used for table interpolation of demodulated data while the per-term angle
+ * used for table interpolation of demodulated data. 1: the per-term angle
  * theta (f - 1/2), f in [0, 1), stays within [-pi, pi], the range of the fast
- * sine and cosine. */
+ * sine and cosine; 2: |theta| up to 256, the angle reduced per term first
+ * (decimation 4 gives theta = 4 pi). */
 static uint32_t turns_q32(double turns)
 {
 	const double fr = turns - std::floor(turns);
@@ -642,8 +643,8 @@ void set_das_rotation(DasParams &p)
 	const double theta = (double)p.r360_fc / (double)p.fs;
 	p.theta = (float)theta;
 	p.theta_half = (float)(0.5 * theta);
-	p.rot_table = p.interp != INTERP_NEAREST && p.fc > 0.0f && std::isfinite(theta) &&
-	              std::fabs(theta) <= 2.0 * M_PI * (1.0 + 1e-6);
+	const bool table = p.interp != INTERP_NEAREST && p.fc > 0.0f && std::isfinite(theta) && std::fabs(theta) <= 256.0;
+	p.rot_table = !table ? 0 : std::fabs(theta) <= 2.0 * M_PI * (1.0 + 1e-6) ? 1 : 2;
 	p.rot_step = p.rot_table ? turns_q32(theta / (2.0 * M_PI)) : 0;
 	p.rot_half = p.rot_table ? turns_q32(theta / (4.0 * M_PI)) : 0;
 }
@@ -727,7 +728,7 @@ int32_t hercules_per_group(const DasParams &p)
 	if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
 	    sms <= 0)
 		sms = 152;
-	const double slots = (double)sms * das_hercules_blocks_per_sm();
+	const double slots = (double)sms * das_hercules_blocks_per_sm(p);
 	const int64_t tiles = das_hercules_tiles(p);
 	const double terms = (double)p.T * p.loop_end / (p.rx_step > 0 ? p.rx_step : 1);
 	double best = 1e30;
