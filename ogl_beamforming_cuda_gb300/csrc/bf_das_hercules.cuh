@@ -210,14 +210,20 @@ __device__ __forceinline__ void hercules_column(const DasParams &p, const float4
 	}
 }
 
-/* One voxel on its own, with the fast or the IEEE square root and divisions. */
+/* One voxel on its own, with the fast or the IEEE square root and divisions (and,
+ * where its sample indices are proven in range, without per-term range tests). */
 template <int INTERP>
 __device__ __forceinline__ void hercules_single(const DasParams &p, const float4 *__restrict__ tab, const HercVoxel &v,
                                              int u_begin, int u_end, float &sx, float &sy)
 {
 	const bool demod = p.fc > 0.0f;
 	const int rot = p.rot_table;
-	if (v.fast) {
+	if (v.fast && v.inrange && INTERP != INTERP_NEAREST) {
+		if (demod && rot == 1)      hercules_column<INTERP, true, true, 1, 1, true>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else if (demod && rot == 2) hercules_column<INTERP, true, true, 2, 1, true>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else if (demod)             hercules_column<INTERP, true, true, 0, 1, true>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else                        hercules_column<INTERP, false, true, 0, 1, true>(p, tab, &v, u_begin, u_end, &sx, &sy);
+	} else if (v.fast) {
 		if (demod && rot == 1)      hercules_column<INTERP, true, true, 1, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
 		else if (demod && rot == 2) hercules_column<INTERP, true, true, 2, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
 		else if (demod)             hercules_column<INTERP, true, true, 0, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
