@@ -434,24 +434,21 @@ def run_precision(args, peaks):
     return 0
 
 
-def run_batched(args, peaks):
-    """Batched variant: 32 seeded acquisitions (transmits {32, 64, 128}, samples
-    {1024, 2048, 4096}, grids from 64x64 planes to 128x128x256 volumes,
-    HERCULES or FORCES), cubic DAS, beamformed by one batch call (graph replay)
-    against the same acquisitions pushed one at a time through the plain API."""
+def _batch_case(args, params, seed0, interp):
+    """One batch of acquisitions: (ms per batch call, host ms one at a time through
+    the plain API, kernel launches per batch call, autotuner report, first call s)."""
     import torch
     from ogl_beamforming_cuda_gb300 import synth, abi
     from ogl_beamforming_cuda_gb300.client import Beamformer
-    torch.cuda.set_device(0)
     SH = abi.SHADER
     pipe = [SH["Decode"], SH["Demodulate"], SH["DAS"]]
     kaiser = synth.kaiser_spec(64)
-    params = synth.batch_workload(7, count=32, interpolate=1)
     rf, out = [], []
     for i, bp in enumerate(params):
-        rf.append(torch.from_numpy(synth.acquisition(bp, 500 + i, n_points=20, n_speckle=200, device="cuda:0")).cuda())
+        rf.append(torch.from_numpy(synth.acquisition(bp, seed0 + i, n_points=20, n_speckle=200, device="cuda:0")).cuda())
         out.append(torch.zeros(2 * int(np.prod(list(bp.output_points)[:3])), dtype=torch.float32, device="cuda:0"))
-    bf = Beamformer().configure(params[0], pipe, kaiser=kaiser, interpolation=1)
+    torch.cuda.synchronize()
+    bf = Beamformer().configure(params[0], pipe, kaiser=kaiser, interpolation=interp)
     stream = torch.cuda.ExternalStream(bf.lib.beamformer_gb300_get_stream())
     bargs = (params, [t.data_ptr() for t in rf], [t.numel() * 2 for t in rf], [t.data_ptr() for t in out])
     t0 = time.perf_counter()
@@ -463,13 +460,13 @@ def run_batched(args, peaks):
     reps = max(args.steps, 1)
     ms_batch = _events_ms(lambda: bf.beamform_batch(*bargs), stream, reps)
     launches = (bf.launches() - l0) // reps
-    tiles, ctas, cand = bf.batch_tuning()
+    tuning = bf.batch_tuning()
     # the same acquisitions one at a time through the plain pipeline (re-planned per acquisition)
-    single = Beamformer().configure(params[0], pipe, kaiser=kaiser, interpolation=1)
+    single = Beamformer().configure(params[0], pipe, kaiser=kaiser, interpolation=interp)
 
     def one_by_one():
         for bp, t in zip(params, rf):
-            single.configure(bp, pipe, kaiser=kaiser, interpolation=1)
+            single.configure(bp, pipe, kaiser=kaiser, interpolation=interp)
             single.push_device(t.data_ptr(), t.numel() * 2)
     one_by_one()
     single.synchronize()
@@ -477,7 +474,26 @@ def run_batched(args, peaks):
     one_by_one()
     single.synchronize()
     ms_single = (time.perf_counter() - h0) * 1e3
+    return ms_batch, ms_single, launches, tuning, build_s
+
+
+def run_batched(args, peaks):
+    """Batched variant: 32 seeded acquisitions (transmits {32, 64, 128}, samples
+    {1024, 2048, 4096}, grids from 64x64 planes to 128x128x256 volumes,
+    HERCULES or FORCES), cubic DAS, beamformed by one batch call (graph replay)
+    against the same acquisitions pushed one at a time through the plain API.
+    A second case of 64 small planes (64x64 and 128x128, 32 or 64 transmits)
+    shows the batch where no single acquisition fills the GPU."""
+    import torch
+    from ogl_beamforming_cuda_gb300 import synth
+    torch.cuda.set_device(0)
+    params = synth.batch_workload(7, count=32, interpolate=1)
+    ms_batch, ms_single, launches, (tiles, ctas, cand), build_s = _batch_case(args, params, 500, 1)
+    small = synth.batch_workload(11, count=64, transmits=(32, 64), samples=(1024, 2048),
+                                 grids=((64, 1, 64), (128, 1, 128)), interpolate=1)
+    sm_batch, sm_single, sm_launches, _, sm_build = _batch_case(args, small, 900, 1)
     vox = [int(np.prod(list(bp.output_points)[:3])) for bp in params]
+    reps = max(args.steps, 1)
     print(json.dumps({
         "metric": "volumes/s of 32 mixed acquisitions, batched vs one at a time", "variant": "batched",
         "value": 32 / (ms_batch / 1e3), "unit": "volumes/s", "n_gpus": 1, "steps": reps, "warmup": args.warmup,
@@ -492,7 +508,12 @@ def run_batched(args, peaks):
                           "how": "configure + push_device per acquisition (the plain API), host-timed"},
         "speedup_vs_one_at_a_time": ms_single / ms_batch,
         "autotuner": {"volume_tiles": tiles, "ctas": ctas, "candidate_ms": [float(x) for x in cand],
-                      "first_call_s": build_s}}))
+                      "first_call_s": build_s},
+        "small_planes": {"workload": "64 acquisitions: transmits {32,64}, samples {1024,2048}, grids {64x1x64, "
+                                     "128x1x128}, HERCULES or FORCES, 128 rx, cubic DAS",
+                         "ms_per_batch": sm_batch, "gpu_launches_per_batch": sm_launches,
+                         "one_at_a_time_ms": sm_single, "speedup_vs_one_at_a_time": sm_single / sm_batch,
+                         "first_call_s": sm_build}}))
     return 0
 
 
