@@ -717,11 +717,15 @@ bool fill_das_params(const Plan &pl, int kind, const void *rf, uint64_t rf_bytes
 }
 
 /* Receive channels per block group of the HERCULES launch. The launch is tiles x
- * groups blocks on SMs x blocks-per-SM slots; when the block count is not a whole
- * number of waves the last wave leaves slots idle (a 128 x 128 x 256 volume is
- * 13.5 waves, a 128 x 128 plane with 16 groups 1.7). The group count is chosen to
- * minimise that idle fraction plus the cost of the partial sums (16 B written and
- * read per voxel and group, against about one term of work per voxel per 2 B). */
+ * groups blocks on SMs x blocks-per-SM slots (the occupancy of the kernel that
+ * runs). The group count minimises, as fractions of the launch:
+ *   - the slots a part-full last wave leaves idle, (waves - w) / waves;
+ *   - the uneven end of the blocks' durations, about half a wave: 0.5 / waves;
+ *   - per group and voxel, the partial sum written and reduced and the voxel's
+ *     set-up, about 12 terms' worth each: 12 G / terms per voxel.
+ * Measured on one GB300: 8 groups for the 128 x 128 x 256 cubic volume (0.7 %
+ * faster than 2, which only removes the part-full wave), 64 for a 128 x 128 plane
+ * (2-7 % faster than 19). */
 int32_t hercules_per_group(const DasParams &p)
 {
 	int dev = 0, sms = 0;
@@ -738,7 +742,7 @@ int32_t hercules_per_group(const DasParams &p)
 		per = (per + p.rx_step - 1) / p.rx_step * p.rx_step;
 		const int32_t G = (p.loop_end + per - 1) / per;
 		const double w = (double)tiles * G / slots, waves = std::ceil(w);
-		const double cost = (waves - w) / waves + (G > 1 ? G * 2.0 / (terms > 1 ? terms : 1) : 0.0);
+		const double cost = (waves - w) / waves + 0.5 / waves + (G > 1 ? G * 12.0 / (terms > 1 ? terms : 1) : 0.0);
 		if (cost < best - 1e-9) {
 			best = cost;
 			best_per = per;
