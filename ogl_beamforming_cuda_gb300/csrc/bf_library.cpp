@@ -769,7 +769,6 @@ bool run_stage(int i, const void *src, uint64_t src_bytes, DeviceFrame &frame, b
 	const int kind = pl.shaders[i];
 	const int out_idx = g.last_chan < 0 ? 0 : 1 - g.last_chan;
 	const int in_idx = g.last_chan < 0 ? 0 : g.last_chan;
-	const BeamformerParameters &bp = g.params;
 	cudaError_t err = cudaSuccess;
 
 	switch (kind) {
