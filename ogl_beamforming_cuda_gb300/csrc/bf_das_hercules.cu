@@ -51,11 +51,12 @@ namespace bf {
  * T2 = (s[n+2] - s[n]) / 2 the segment is a0 + a1 f + a2 f^2 + a3 f^3 with
  * a0 = P1, a1 = T1, a2 = 3 (P2 - P1) - 2 T1 - T2, a3 = 2 (P1 - P2) + T1 + T2;
  * stored as float4 (a0, a1) and float4 (a2, a3), complex pairs.
- * Linear: float4 (s[n], s[n+1] - s[n]).
+ * Linear: float4 (s[n], s[n+1] - s[n]). Nearest (ROT only): float2 s[n].
  * ROT: every coefficient of the segment starting at sample j = n mod S of its row
  * is multiplied by exp(i theta (j + 1/2)), the demodulation phase at the middle of
- * the segment, from its turns (j * rot_step + rot_half) / 2^32 (0.32 fixed point:
- * the product wraps exactly; the phase error is at most (j + 1) * 2^-33 turns). */
+ * the segment (nearest: exp(i theta j), rot_half = 0), from its turns
+ * (j * rot_step + rot_half) / 2^32 (0.32 fixed point: the product wraps exactly;
+ * the phase error is at most (j + 1) * 2^-33 turns). */
 template <int INTERP, bool ROT>
 __global__ void __launch_bounds__(256)
 interp_table(const float2 *__restrict__ rf, int64_t entries, int64_t readable, int32_t S, uint32_t rot_step,
@@ -72,6 +73,10 @@ interp_table(const float2 *__restrict__ rf, int64_t entries, int64_t readable, i
 		}
 		/* (x + i y) exp(i phi) */
 		auto rot = [&](float x, float y) { return make_float2(cs * x - sn * y, sn * x + cs * y); };
+		if (INTERP == INTERP_NEAREST) {
+			((float2 *)out)[n] = rot(s1.x, s1.y);
+			continue;
+		}
 		if (INTERP == INTERP_LINEAR) {
 			const float2 a0 = ROT ? rot(s1.x, s1.y) : s1;
 			const float2 a1 = ROT ? rot(s2.x - s1.x, s2.y - s1.y) : make_float2(s2.x - s1.x, s2.y - s1.y);
@@ -112,7 +117,8 @@ das_hercules(DasParams p, const float4 *__restrict__ tab)
 int64_t das_hercules_table_entries(const DasParams &p)
 {
 	const int64_t n = (int64_t)p.C * p.T * p.S;
-	return p.interp == INTERP_CUBIC ? 2 * n : p.interp == INTERP_LINEAR ? n : 0;
+	/* float4 entries; nearest holds float2 samples, only when they are rotated */
+	return p.interp == INTERP_CUBIC ? 2 * n : p.interp == INTERP_LINEAR ? n : p.rot_table ? (n + 1) / 2 : 0;
 }
 
 int64_t das_hercules_tiles(const DasParams &p)
@@ -169,12 +175,14 @@ static void launch_hercules_tiles(const DasParams &p, const float4 *table, cudaS
 
 cudaError_t launch_das_table(const DasParams &p, float4 *table, cudaStream_t s)
 {
-	if (p.interp == INTERP_NEAREST) return cudaSuccess;
+	if (das_hercules_table_entries(p) == 0) return cudaSuccess;
 	if (!table) return cudaErrorInvalidValue;
 	const int64_t entries = (int64_t)p.C * p.T * p.S;
 	const int blocks = (int)((entries + 255) / 256 < 152 * 16 ? (entries + 255) / 256 : 152 * 16);
 	const bool rot = p.rot_table != 0;
-	if (p.interp == INTERP_CUBIC) {
+	if (p.interp == INTERP_NEAREST) {
+		interp_table<INTERP_NEAREST, true><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, p.S, p.rot_step, 0, table);
+	} else if (p.interp == INTERP_CUBIC) {
 		if (rot) interp_table<INTERP_CUBIC, true><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, p.S, p.rot_step, p.rot_half, table);
 		else     interp_table<INTERP_CUBIC, false><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, p.S, 0, 0, table);
 	} else {
@@ -190,9 +198,9 @@ cudaError_t launch_das_hercules(const DasParams &p, float4 *table, cudaStream_t 
 	const int64_t n = (int64_t)p.dims[0] * p.dims[1] * p.dims[2];
 	if (n == 0) return cudaSuccess;
 	if (!das_hercules_supported(p) || p.groups < 1 || (p.groups > 1 && !p.partial) || p.rx_step < 1 ||
-	    (p.interp != INTERP_NEAREST && !table))
+	    (das_hercules_table_entries(p) > 0 && !table))
 		return cudaErrorInvalidValue;
-	if (p.interp != INTERP_NEAREST) {
+	if (das_hercules_table_entries(p) > 0) {
 		const cudaError_t e = launch_das_table(p, table, s);
 		if (e != cudaSuccess) return e;
 	}

@@ -58,7 +58,16 @@ __device__ __forceinline__ void term_tail(const DasParams &p, const float4 *__re
 	const float a  = ok ? apod_cos2_p5(w) * scale : 0.0f;
 	const float ic = ok ? idx : 1.0f;
 	float vx, vy, f = 0.0f;
-	if (INTERP == INTERP_NEAREST) {
+	if (INTERP == INTERP_NEAREST && INR) {
+		/* round(idx) proven inside the row: no bound check; with ROT the sample
+		 * comes pre-rotated by its phase from the table (float2 per sample) */
+		const float r = roundf(ic);
+		const int j = row + (int)r;
+		const float2 v = ROT != 0 ? __ldg((const float2 *)tab + j) : __ldg(p.rf + j);
+		vx = v.x;
+		vy = v.y;
+		f = ic - r;                                         /* in [-1/2, 1/2] */
+	} else if (INTERP == INTERP_NEAREST) {
 		const int j = row + (int)roundf(ic);
 		const int last = (int)p.rf_count - 1;
 		float2 v = __ldg(p.rf + min(j, last));
@@ -83,8 +92,9 @@ __device__ __forceinline__ void term_tail(const DasParams &p, const float4 *__re
 	}
 	if (DEMOD) {
 		float sn, cs;
-		if (ROT != 0 && INTERP != INTERP_NEAREST) {
-			float a = fmaf(p.theta, f, -p.theta_half);
+		if (ROT != 0 && (INTERP != INTERP_NEAREST || INR)) {
+			/* table interpolation: theta (f - 1/2); nearest: theta (idx - round(idx)) */
+			float a = INTERP == INTERP_NEAREST ? __fmul_rn(p.theta, f) : fmaf(p.theta, f, -p.theta_half);
 			if (ROT == 2) {
 				/* two-constant split of 2 pi: off by at most |k| * 1.1e-11 rad */
 				const float k = rintf(a * 0.159154943f);
@@ -114,7 +124,7 @@ struct HercVoxel {
 	float q_fix, q_var;     /* lateral coordinates fixed by r and varied by t */
 	float dz2, dtx, ka2, lim2;
 	bool  fast;             /* every term inside the verified fast-math ranges */
-	bool  inrange;          /* every term's sample index inside [0, S - 2) (cubic) / [0, S - 1) (linear) */
+	bool  inrange;          /* every term's sample index inside [0, S - 2) (cubic), [0, S - 1) (linear), [0, S - 1/2) (nearest) */
 };
 
 __device__ __forceinline__ HercVoxel hercules_setup(const DasParams &p, int vx, int vy, int vz)
@@ -147,9 +157,11 @@ __device__ __forceinline__ HercVoxel hercules_setup(const DasParams &p, int vx, 
 	 * samples) cover the roundings of the term's chain and of these bounds */
 	const float dmin = v.dtx + sqrtf(v.dz2) * 0.9999f, dmax = v.dtx + sqrtf(xmax) * 1.0001f;
 	const float imin = (dmin / p.c + p.toff) * p.fs, imax = (dmax / p.c + p.toff) * p.fs;
-	const float s_lim = (float)(p.S - (p.interp == INTERP_CUBIC ? 2 : 1));
-	v.inrange = p.interp != INTERP_NEAREST && p.c > 0.0f && p.fs > 0.0f &&
-	            imin - fabsf(imin) * 1e-4f >= 0.01f && imax + fabsf(imax) * 1e-4f + 0.01f < s_lim;
+	/* nearest: round(idx) <= S - 1 needs idx < S - 1/2 */
+	const float s_lim = p.interp == INTERP_CUBIC ? (float)(p.S - 2) : p.interp == INTERP_LINEAR ? (float)(p.S - 1)
+	                                                                                         : (float)p.S - 0.5f;
+	v.inrange = p.c > 0.0f && p.fs > 0.0f && imin - fabsf(imin) * 1e-4f >= 0.01f &&
+	            imax + fabsf(imax) * 1e-4f + 0.01f < s_lim;
 	return v;
 }
 
@@ -218,7 +230,7 @@ __device__ __forceinline__ void hercules_single(const DasParams &p, const float4
 {
 	const bool demod = p.fc > 0.0f;
 	const int rot = p.rot_table;
-	if (v.fast && v.inrange && INTERP != INTERP_NEAREST) {
+	if (v.fast && v.inrange) {
 		if (demod && rot == 1)      hercules_column<INTERP, true, true, 1, 1, true>(p, tab, &v, u_begin, u_end, &sx, &sy);
 		else if (demod && rot == 2) hercules_column<INTERP, true, true, 2, 1, true>(p, tab, &v, u_begin, u_end, &sx, &sy);
 		else if (demod)             hercules_column<INTERP, true, true, 0, 1, true>(p, tab, &v, u_begin, u_end, &sx, &sy);
@@ -279,7 +291,7 @@ __device__ __forceinline__ void hercules_tile(const DasParams &p, const float4 *
 	if (NV > 1 && together && fast) {
 		const bool demod = p.fc > 0.0f;
 		const int rot = p.rot_table;
-		bool inr = INTERP != INTERP_NEAREST;
+		bool inr = true;
 		#pragma unroll
 		for (int k = 0; k < NV; k++) inr = inr && v[k].inrange;
 		if (inr) {

@@ -628,10 +628,11 @@ void fill_filter_params(const Plan &pl, int i, const void *src, uint64_t src_byt
 }
 
 /* Phase rotation of the HERCULES interpolation table (DasParams::rot_table):
- * used for table interpolation of demodulated data. 1: the per-term angle
- * theta (f - 1/2), f in [0, 1), stays within [-pi, pi], the range of the fast
- * sine and cosine; 2: |theta| up to 256, the angle reduced per term first
- * (decimation 4 gives theta = 4 pi). */
+ * used for demodulated data. 1: the per-term angle theta (f - 1/2), f in
+ * [0, 1) (nearest: theta (idx - round(idx))), stays within [-pi, pi], the range
+ * of the fast sine and cosine; 2: |theta| up to 256, the angle reduced per term
+ * first (decimation 4 gives theta = 4 pi). Nearest interpolation uses the rotated
+ * samples only for voxels whose indices are proven in range. */
 static uint32_t turns_q32(double turns)
 {
 	const double fr = turns - std::floor(turns);
@@ -643,10 +644,11 @@ void set_das_rotation(DasParams &p)
 	const double theta = (double)p.r360_fc / (double)p.fs;
 	p.theta = (float)theta;
 	p.theta_half = (float)(0.5 * theta);
-	const bool table = p.interp != INTERP_NEAREST && p.fc > 0.0f && std::isfinite(theta) && std::fabs(theta) <= 256.0;
+	const bool table = p.fc > 0.0f && std::isfinite(theta) && std::fabs(theta) <= 256.0;
 	p.rot_table = !table ? 0 : std::fabs(theta) <= 2.0 * M_PI * (1.0 + 1e-6) ? 1 : 2;
 	p.rot_step = p.rot_table ? turns_q32(theta / (2.0 * M_PI)) : 0;
-	p.rot_half = p.rot_table ? turns_q32(theta / (4.0 * M_PI)) : 0;
+	/* segments are rotated at their middle (j + 1/2), nearest samples at j */
+	p.rot_half = p.rot_table && p.interp != INTERP_NEAREST ? turns_q32(theta / (4.0 * M_PI)) : 0;
 }
 
 /* DAS stage of a plan reading channel data rf (rf_bytes readable) into frame
@@ -1148,7 +1150,7 @@ cudaError_t batch_launch(cudaStream_t s)
 			if (e != cudaSuccess) return e;
 			last = out_idx;
 		}
-		if (a.path != DAS_BATCH_GENERIC && a.das.interp != INTERP_NEAREST) {
+		if (a.path != DAS_BATCH_GENERIC && das_hercules_table_entries(a.das) > 0) {
 			const cudaError_t e = launch_das_table(a.das, a.das_table, s);
 			if (e != cudaSuccess) return e;
 		}

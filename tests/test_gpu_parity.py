@@ -138,12 +138,14 @@ def test_das_hercules_plane_32_channels(interp):
     check_volume(bf.frame(0)[0], ref["frame"], f"HERCULES DASFast 32x32 interp={interp}")
 
 
-@pytest.mark.parametrize("interp", (1, 2))
+@pytest.mark.parametrize("interp", (0, 1, 2))
 @pytest.mark.parametrize("fc_scale", (0.5, 0.77, 1.0, 1.3, 2.0))
 def test_das_hercules_phase_paths(interp, fc_scale):
-    """Demodulation phase of the table path: theta = 2 pi fc / fs up to 2 pi puts
-    the integer sample's phase into the interpolation table (the bench has theta =
-    2 pi exactly); above 2 pi the term computes the reference's angle."""
+    """Demodulation phase of the table path: the phase of the integer sample (cubic
+    and linear: of the segment's middle) sits in the per-frame table and the term
+    rotates by the rest (the bench has theta = 2 pi fc / fs = 2 pi exactly; above
+    2 pi that angle is reduced first). Nearest uses rotated samples for voxels
+    whose indices are proven in range and the reference's angle elsewhere."""
     bp = small_params(S=2048, C=16, T=16, points=(24, 2, 48), D=2)
     bp.center_frequency *= fc_scale
     raw = small_raw(bp, n_points=12, n_speckle=300)
