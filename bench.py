@@ -388,6 +388,7 @@ def run_precision(args, peaks):
     for prec, name in ((0, "fp32"), (1, "fp16"), (2, "bf16")):
         bf = Beamformer().configure(bp, pipe, kaiser=kaiser, interpolation=2)
         assert bf.lib.beamformer_gb300_set_filter_precision(prec)
+        assert bf.lib.beamformer_gb300_set_das_precision(1 if prec else 0)
         stream = torch.cuda.ExternalStream(bf.lib.beamformer_gb300_get_stream())
         push = lambda: bf.push_device(raw.data_ptr(), raw.numel() * 2)
         for _ in range(max(args.warmup, 3)):
@@ -397,6 +398,8 @@ def run_precision(args, peaks):
         res[name] = {"frames_per_s": 1e3 / ms, "ms_per_frame": ms, "stage_ms": {k: v * 1e3 for k, v in
                                                                                 stage_times(bf, 20).items()},
                      "channel_data": bf.channel_data().copy(), "frame": bf.frame(0)[0].copy(), "bf": bf}
+    bf.lib.beamformer_gb300_set_filter_precision(0)
+    bf.lib.beamformer_gb300_set_das_precision(0)
     errors = None
     if not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -422,16 +425,56 @@ def run_precision(args, peaks):
     for v in res.values():
         for k in ("channel_data", "frame", "bf"):
             v.pop(k)
+    vol3d = _precision_volume(args)
     print(json.dumps({
         "metric": "frames/s of the precision variant (decode + demodulate + DAS, plane)", "variant": "precision",
         "value": res["bf16"]["frames_per_s"], "unit": "frames/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "higher_is_better": True, "dtype": "fp16/bf16 operands, f32 accumulate",
+        "warmup": args.warmup, "higher_is_better": True,
+        "dtype": "fp16/bf16 front-end operands, fp16 DAS table, f32 accumulate",
         "data": "synthetic (seeded RF generator)",
         "config": {"workload": "HERCULES plane 128x1x128, 128 tx, 128 rx, 4096 int16 samples, 128-tap Kaiser, "
-                               "decimation 2, linear DAS", "l2": "one 134 MB frame per push, larger than L2"},
+                               "decimation 2, linear DAS", "l2": "one 134 MB frame per push, larger than L2",
+                   "das_precision": "1 (fp16 table) for fp16 and bf16, 0 for fp32"},
         "per_precision": res, "errors": errors,
-        "speedup_vs_fp32": {k: res[k]["frames_per_s"] / res["fp32"]["frames_per_s"] for k in res}}))
+        "speedup_vs_fp32": {k: res[k]["frames_per_s"] / res["fp32"]["frames_per_s"] for k in res},
+        "volume_3d": vol3d}))
     return 0
+
+
+def _precision_volume(args):
+    """The 3D workload (16 frames per volume, cubic DAS 128 x 128 x 256) in FP32
+    and mixed (FP16 front end, FP16 DAS table): volumes/s of each, per-stage times
+    and the mixed volume's NRMSE against the FP32 volume (itself within -80 dB of
+    the oracle)."""
+    import torch
+    from ogl_beamforming_cuda_gb300.client import Beamformer
+    bp, pipe, kaiser = workload()
+    frames = frames_on_device(bp, "cuda:0", speckle=args.speckle)
+    nbytes = frames[0].numel() * 2
+    out, vols = {}, {}
+    for name, fp, dp in (("fp32", 0, 0), ("mixed", 1, 1)):
+        bf = Beamformer().configure(bp, pipe, kaiser=kaiser)
+        assert bf.lib.beamformer_gb300_set_filter_precision(fp)
+        assert bf.lib.beamformer_gb300_set_das_precision(dp)
+        stream = torch.cuda.ExternalStream(bf.lib.beamformer_gb300_get_stream())
+
+        def step():
+            for f in range(FRAMES):
+                bf.push_device(frames[f].data_ptr(), nbytes)
+        for _ in range(max(args.warmup, 3)):
+            step()
+        bf.synchronize()
+        ms = _events_ms(step, stream, max(args.steps, 1))
+        vols[name] = bf.frame(0)[0].copy()
+        out[name] = {"volumes_per_s": 1e3 / ms, "ms_per_volume": ms,
+                     "stage_ms": {k: v * 1e3 for k, v in stage_times(bf, FRAMES).items()}}
+    bf.lib.beamformer_gb300_set_filter_precision(0)
+    bf.lib.beamformer_gb300_set_das_precision(0)
+    a, b = vols["mixed"].astype(np.float64), vols["fp32"].astype(np.float64)
+    out["mixed"]["volume_db_vs_fp32"] = float(20 * np.log10(np.sqrt(np.mean((a - b) ** 2) / np.mean(b ** 2))))
+    out["speedup_vs_fp32"] = out["mixed"]["volumes_per_s"] / out["fp32"]["volumes_per_s"]
+    out["workload"] = config_dict()["workload"]
+    return out
 
 
 def _batch_case(args, params, seed0, interp):

@@ -344,6 +344,17 @@ LIB_FN uint32_t beamformer_gb300_set_interpolation(int32_t mode);
  * while a 16-bit precision is selected. Takes effect at the next compute. */
 LIB_FN uint32_t beamformer_gb300_set_filter_precision(int32_t precision);
 
+/* Arithmetic of HERCULES delay-and-sum (no counterpart in the reference; the
+ * precision variant): 0 = FP32 with the reference's sample indices (default);
+ * 1 = the per-frame interpolation table in FP16 (coefficients scaled by a power
+ * of two from the frame's largest channel-data magnitude, evaluated in packed
+ * FP16), the sample index from an approximate square root and one FMA, and a
+ * degree-3 apodization polynomial, with FP32 sums. Applies where DAS runs on the
+ * HERCULES fast path (DASFast; dense channel data, no sparse elements, no
+ * coherency weighting); other DAS stages stay FP32. beamformer_gb300_beamform_batch
+ * fails with UNSUPPORTED while 1 is selected. Takes effect at the next compute. */
+LIB_FN uint32_t beamformer_gb300_set_das_precision(int32_t precision);
+
 /* Receive-aperture subsampling of HERCULES delay-and-sum (no counterpart in the
  * reference; the input of the learned variant): DAS sums receive channels 0,
  * step, 2 step, ... only (step 1, the default, uses all). Other DAS modes fail

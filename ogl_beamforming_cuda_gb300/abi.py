@@ -100,6 +100,7 @@ SIGNATURES = [
     ("beamformer_gb300_get_filter", u32, [ctypes.c_uint8, P(f32), i32, P(i32)]),
     ("beamformer_gb300_set_interpolation", u32, [i32]),
     ("beamformer_gb300_set_filter_precision", u32, [i32]),
+    ("beamformer_gb300_set_das_precision", u32, [i32]),
     ("beamformer_gb300_set_receive_subsampling", u32, [i32]),
     ("beamformer_gb300_serve", i32, [i32]),
     ("beamformer_gb300_serve_stop", None, []),

@@ -57,12 +57,37 @@ namespace bf {
  * the segment (nearest: exp(i theta j), rot_half = 0), from its turns
  * (j * rot_step + rot_half) / 2^32 (0.32 fixed point: the product wraps exactly;
  * the phase error is at most (j + 1) * 2^-33 turns). */
-template <int INTERP, bool ROT>
+/* Largest |component| of the channel data rf[0, n), as float bits into *out
+ * (zeroed before; NaN components are skipped): the scale of the FP16 table. */
+__global__ void __launch_bounds__(256)
+chan_absmax(const float2 *__restrict__ rf, int64_t n, unsigned *__restrict__ out)
+{
+	float m = 0.0f;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const float2 v = __ldg(rf + i);
+		m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
+	}
+	/* non-negative floats order as their bit patterns */
+	const unsigned b = __reduce_max_sync(0xffffffffu, __float_as_uint(m));
+	if ((threadIdx.x & 31) == 0 && b) atomicMax(out, b);
+}
+
+/* H: DAS precision 1, every complex coefficient times 2^k (half_table_shift of
+ * *absmax) rounded to an FP16 pair: cubic 16 bytes (a0, a1, a2, a3), linear 8
+ * bytes (a0, a1), nearest 4 bytes (rotated or not). */
+template <int INTERP, bool ROT, bool H = false>
 __global__ void __launch_bounds__(256)
 interp_table(const float2 *__restrict__ rf, int64_t entries, int64_t readable, int32_t S, uint32_t rot_step,
-             uint32_t rot_half, float4 *__restrict__ out)
+             uint32_t rot_half, const unsigned *__restrict__ absmax, float4 *__restrict__ out)
 {
 	const float2 zero = make_float2(0.0f, 0.0f);
+	const float hs = H ? pow2f(half_table_shift(__ldg(absmax))) : 1.0f;
+	auto h2 = [&](float2 a) {
+		const __half2 h = __floats2half2_rn(a.x * hs, a.y * hs);
+		unsigned u;
+		memcpy(&u, &h, sizeof(u));
+		return u;
+	};
 	for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < entries; n += (int64_t)gridDim.x * blockDim.x) {
 		const float2 s1 = n < readable ? rf[n] : zero;
 		const float2 s2 = n + 1 < readable ? rf[n + 1] : zero;
@@ -74,13 +99,16 @@ interp_table(const float2 *__restrict__ rf, int64_t entries, int64_t readable, i
 		/* (x + i y) exp(i phi) */
 		auto rot = [&](float x, float y) { return make_float2(cs * x - sn * y, sn * x + cs * y); };
 		if (INTERP == INTERP_NEAREST) {
-			((float2 *)out)[n] = rot(s1.x, s1.y);
+			const float2 a0 = ROT ? rot(s1.x, s1.y) : s1;
+			if (H) ((unsigned *)out)[n] = h2(a0);
+			else   ((float2 *)out)[n] = a0;
 			continue;
 		}
 		if (INTERP == INTERP_LINEAR) {
 			const float2 a0 = ROT ? rot(s1.x, s1.y) : s1;
 			const float2 a1 = ROT ? rot(s2.x - s1.x, s2.y - s1.y) : make_float2(s2.x - s1.x, s2.y - s1.y);
-			out[n] = make_float4(a0.x, a0.y, a1.x, a1.y);
+			if (H) ((uint2 *)out)[n] = make_uint2(h2(a0), h2(a1));
+			else   out[n] = make_float4(a0.x, a0.y, a1.x, a1.y);
 			continue;
 		}
 		const float2 s0 = n > 0 && n - 1 < readable ? rf[n - 1] : zero;
@@ -97,8 +125,12 @@ interp_table(const float2 *__restrict__ rf, int64_t entries, int64_t readable, i
 			a2 = rot(a2.x, a2.y);
 			a3 = rot(a3.x, a3.y);
 		}
-		out[2 * n]     = make_float4(a0.x, a0.y, a1.x, a1.y);
-		out[2 * n + 1] = make_float4(a2.x, a2.y, a3.x, a3.y);
+		if (H) {
+			((uint4 *)out)[n] = make_uint4(h2(a0), h2(a1), h2(a2), h2(a3));
+		} else {
+			out[2 * n]     = make_float4(a0.x, a0.y, a1.x, a1.y);
+			out[2 * n + 1] = make_float4(a2.x, a2.y, a3.x, a3.y);
+		}
 	}
 }
 
@@ -106,19 +138,21 @@ interp_table(const float2 *__restrict__ rf, int64_t entries, int64_t readable, i
  * slower (96.4 against 94.9 ms per 128 x 128 x 256 cubic frame) */
 template <int TY> __host__ __device__ constexpr int herc_threads() { return 128; }
 
-template <int INTERP, int TY>
+template <int INTERP, int TY, bool H>
 __global__ void __launch_bounds__(herc_threads<TY>(), 1024 / herc_threads<TY>())
 das_hercules(DasParams p, const float4 *__restrict__ tab)
 {
 	const int yt = blockIdx.y / p.groups;
-	hercules_tile<INTERP, TY, herc_threads<TY>()>(p, tab, blockIdx.x, yt, blockIdx.z, blockIdx.y - yt * p.groups);
+	hercules_tile<INTERP, TY, herc_threads<TY>(), H>(p, tab, blockIdx.x, yt, blockIdx.z, blockIdx.y - yt * p.groups);
 }
 
-int64_t das_hercules_table_entries(const DasParams &p)
+int64_t das_hercules_table_bytes(const DasParams &p)
 {
 	const int64_t n = (int64_t)p.C * p.T * p.S;
-	/* float4 entries; nearest holds float2 samples, only when they are rotated */
-	return p.interp == INTERP_CUBIC ? 2 * n : p.interp == INTERP_LINEAR ? n : p.rot_table ? (n + 1) / 2 : 0;
+	/* FP32: cubic 32 bytes per sample, linear 16, nearest 8 (only rotated data);
+	 * FP16 (precision 1): half of that, nearest always */
+	if (p.half_table) return p.interp == INTERP_CUBIC ? 16 * n : p.interp == INTERP_LINEAR ? 8 * n : 4 * n;
+	return p.interp == INTERP_CUBIC ? 32 * n : p.interp == INTERP_LINEAR ? 16 * n : p.rot_table ? 8 * n : 0;
 }
 
 int64_t das_hercules_tiles(const DasParams &p)
@@ -132,25 +166,27 @@ int64_t das_hercules_tiles(const DasParams &p)
 	return (int64_t)((p.dims[0] + T::X - 1) / T::X) * p.dims[1] * ((p.dims[2] + T::Z * T::NV - 1) / (T::Z * T::NV));
 }
 
-template <int TY>
+template <int TY, bool H>
 static int hercules_occupancy(int interp)
 {
 	int n = 0;
 	cudaError_t e;
 	switch (interp) {
-	case INTERP_CUBIC:  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, das_hercules<INTERP_CUBIC, TY>, herc_threads<TY>(), 0); break;
-	case INTERP_LINEAR: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, das_hercules<INTERP_LINEAR, TY>, herc_threads<TY>(), 0); break;
-	default:            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, das_hercules<INTERP_NEAREST, TY>, herc_threads<TY>(), 0); break;
+	case INTERP_CUBIC:  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, das_hercules<INTERP_CUBIC, TY, H>, herc_threads<TY>(), 0); break;
+	case INTERP_LINEAR: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, das_hercules<INTERP_LINEAR, TY, H>, herc_threads<TY>(), 0); break;
+	default:            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, das_hercules<INTERP_NEAREST, TY, H>, herc_threads<TY>(), 0); break;
 	}
 	return e == cudaSuccess && n > 0 ? n : 1024 / herc_threads<TY>();
 }
 
 int das_hercules_blocks_per_sm(const DasParams &p)
 {
-	static int cache[2][3] = {};
-	const int ty = p.dims[1] >= 4 ? 1 : 0, ip = p.interp >= 0 && p.interp < 3 ? p.interp : 0;
-	if (!cache[ty][ip]) cache[ty][ip] = ty ? hercules_occupancy<4>(p.interp) : hercules_occupancy<1>(p.interp);
-	return cache[ty][ip];
+	static int cache[2][3][2] = {};
+	const int ty = p.dims[1] >= 4 ? 1 : 0, ip = p.interp >= 0 && p.interp < 3 ? p.interp : 0, h = p.half_table ? 1 : 0;
+	int &c = cache[ty][ip][h];
+	if (!c) c = ty ? (h ? hercules_occupancy<4, true>(p.interp) : hercules_occupancy<4, false>(p.interp))
+	               : (h ? hercules_occupancy<1, true>(p.interp) : hercules_occupancy<1, false>(p.interp));
+	return c;
 }
 
 bool das_hercules_supported(const DasParams &p)
@@ -159,7 +195,7 @@ bool das_hercules_supported(const DasParams &p)
 	       p.rf_count >= (int64_t)p.C * p.T * p.S && p.loop_end == p.C;
 }
 
-template <int TY>
+template <int TY, bool H>
 static void launch_hercules_tiles(const DasParams &p, const float4 *table, cudaStream_t s)
 {
 	constexpr int THREADS = herc_threads<TY>();
@@ -167,27 +203,43 @@ static void launch_hercules_tiles(const DasParams &p, const float4 *table, cudaS
 	dim3 grid((p.dims[0] + Tile::X - 1) / Tile::X, ((p.dims[1] + Tile::Y - 1) / Tile::Y) * p.groups,
 	          (p.dims[2] + Tile::Z * Tile::NV - 1) / (Tile::Z * Tile::NV));
 	switch (p.interp) {
-	case INTERP_CUBIC:  das_hercules<INTERP_CUBIC, TY><<<grid, THREADS, 0, s>>>(p, table); break;
-	case INTERP_LINEAR: das_hercules<INTERP_LINEAR, TY><<<grid, THREADS, 0, s>>>(p, table); break;
-	default:            das_hercules<INTERP_NEAREST, TY><<<grid, THREADS, 0, s>>>(p, table); break;
+	case INTERP_CUBIC:  das_hercules<INTERP_CUBIC, TY, H><<<grid, THREADS, 0, s>>>(p, table); break;
+	case INTERP_LINEAR: das_hercules<INTERP_LINEAR, TY, H><<<grid, THREADS, 0, s>>>(p, table); break;
+	default:            das_hercules<INTERP_NEAREST, TY, H><<<grid, THREADS, 0, s>>>(p, table); break;
+	}
+}
+
+template <bool H>
+static void launch_table(const DasParams &p, int64_t entries, int blocks, float4 *table, cudaStream_t s)
+{
+	const bool rot = p.rot_table != 0;
+	const uint32_t step = rot ? p.rot_step : 0, half = rot ? p.rot_half : 0;
+	switch (p.interp * 2 + (rot ? 1 : 0)) {
+	case INTERP_NEAREST * 2 + 1: interp_table<INTERP_NEAREST, true, H><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, p.S, step, 0, p.absmax, table); break;
+	case INTERP_NEAREST * 2:     interp_table<INTERP_NEAREST, false, H><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, p.S, 0, 0, p.absmax, table); break;
+	case INTERP_CUBIC * 2 + 1:   interp_table<INTERP_CUBIC, true, H><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, p.S, step, half, p.absmax, table); break;
+	case INTERP_CUBIC * 2:       interp_table<INTERP_CUBIC, false, H><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, p.S, 0, 0, p.absmax, table); break;
+	case INTERP_LINEAR * 2 + 1:  interp_table<INTERP_LINEAR, true, H><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, p.S, step, half, p.absmax, table); break;
+	default:                     interp_table<INTERP_LINEAR, false, H><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, p.S, 0, 0, p.absmax, table); break;
 	}
 }
 
 cudaError_t launch_das_table(const DasParams &p, float4 *table, cudaStream_t s)
 {
-	if (das_hercules_table_entries(p) == 0) return cudaSuccess;
-	if (!table) return cudaErrorInvalidValue;
+	if (das_hercules_table_bytes(p) == 0) return cudaSuccess;
+	if (!table || (p.half_table && !p.absmax)) return cudaErrorInvalidValue;
 	const int64_t entries = (int64_t)p.C * p.T * p.S;
 	const int blocks = (int)((entries + 255) / 256 < 152 * 16 ? (entries + 255) / 256 : 152 * 16);
-	const bool rot = p.rot_table != 0;
-	if (p.interp == INTERP_NEAREST) {
-		interp_table<INTERP_NEAREST, true><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, p.S, p.rot_step, 0, table);
-	} else if (p.interp == INTERP_CUBIC) {
-		if (rot) interp_table<INTERP_CUBIC, true><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, p.S, p.rot_step, p.rot_half, table);
-		else     interp_table<INTERP_CUBIC, false><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, p.S, 0, 0, table);
+	if (p.half_table) {
+		/* the scale: every sample the table reads, rf[0, min(readable, entries + 2)) */
+		const int64_t n = p.rf_count < entries + 2 ? p.rf_count : entries + 2;
+		cudaError_t e = cudaMemsetAsync(p.absmax, 0, sizeof(unsigned), s);
+		if (e != cudaSuccess) return e;
+		chan_absmax<<<blocks, 256, 0, s>>>(p.rf, n, p.absmax);
+		g_kernel_launches++;
+		launch_table<true>(p, entries, blocks, table, s);
 	} else {
-		if (rot) interp_table<INTERP_LINEAR, true><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, p.S, p.rot_step, p.rot_half, table);
-		else     interp_table<INTERP_LINEAR, false><<<blocks, 256, 0, s>>>(p.rf, entries, p.rf_count, p.S, 0, 0, table);
+		launch_table<false>(p, entries, blocks, table, s);
 	}
 	g_kernel_launches++;
 	return cudaGetLastError();
@@ -198,14 +250,19 @@ cudaError_t launch_das_hercules(const DasParams &p, float4 *table, cudaStream_t 
 	const int64_t n = (int64_t)p.dims[0] * p.dims[1] * p.dims[2];
 	if (n == 0) return cudaSuccess;
 	if (!das_hercules_supported(p) || p.groups < 1 || (p.groups > 1 && !p.partial) || p.rx_step < 1 ||
-	    (das_hercules_table_entries(p) > 0 && !table))
+	    (das_hercules_table_bytes(p) > 0 && !table) || (p.half_table && !p.absmax))
 		return cudaErrorInvalidValue;
-	if (das_hercules_table_entries(p) > 0) {
+	if (das_hercules_table_bytes(p) > 0) {
 		const cudaError_t e = launch_das_table(p, table, s);
 		if (e != cudaSuccess) return e;
 	}
-	if (p.dims[1] >= 4) launch_hercules_tiles<4>(p, table, s);
-	else                launch_hercules_tiles<1>(p, table, s);
+	if (p.half_table) {
+		if (p.dims[1] >= 4) launch_hercules_tiles<4, true>(p, table, s);
+		else                launch_hercules_tiles<1, true>(p, table, s);
+	} else {
+		if (p.dims[1] >= 4) launch_hercules_tiles<4, false>(p, table, s);
+		else                launch_hercules_tiles<1, false>(p, table, s);
+	}
 	g_kernel_launches++;
 	if (p.groups > 1) {
 		cudaError_t e = cudaGetLastError();

@@ -4,6 +4,7 @@
  * column loop over receive channels and transmits, and one voxel tile.
  */
 #pragma once
+#include <cuda_fp16.h>
 #include "bf_kernels.h"
 #include "bf_das_math.cuh"
 
@@ -34,6 +35,39 @@ __device__ __forceinline__ float apod_cos2_p5(float w)
 	return fmaf(c, w, 1.0f);
 }
 
+/* cos^2(sqrt(w)) on [0, (pi/2)^2] for DAS precision 1: (1 - w / (pi/2)^2)
+ * (1 + a w + b w^2) expanded, a and b a weighted least-squares fit iterated towards
+ * the minimax error; maximum absolute error 9.6e-4, 1.2e-7 at the aperture edge.
+ * Three FMAs. */
+__device__ __forceinline__ float apod_cos2_p3(float w)
+{
+	float c = -0.031044068f;
+	c = fmaf(c, w, 0.31450406f);
+	c = fmaf(c, w, -0.99229395f);
+	return fmaf(c, w, 1.0f);
+}
+
+/* Table scale of DAS precision 1: the shift k with m 2^k in [1024, 2048) for the
+ * largest channel-data magnitude m (float bits); 0 when m is 0, below 2^-100,
+ * above 2^100 or not a number. Every FP16 coefficient and Horner partial sum is
+ * then below 17 m 2^k < 2^15 (the cubic coefficients sum to at most 17 m). */
+__device__ __forceinline__ int half_table_shift(unsigned m_bits)
+{
+	const float m = __uint_as_float(m_bits);
+	if (!(m >= 0x1p-100f && m <= 0x1p100f)) return 0;
+	const int e = (int)((m_bits >> 23) & 0xffu) - 126;   /* m = f 2^e, f in [1/2, 1) */
+	return 11 - e;
+}
+
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }
+
+__device__ __forceinline__ __half2 as_half2(unsigned u)
+{
+	__half2 h;
+	memcpy(&h, &u, sizeof(h));
+	return h;
+}
+
 /* The part of one (voxel, transmit t, receive r) term after the lateral distance:
  * lat2 = |lateral offset|^2 of the virtual element (r, t); row = (r * T + t) * S.
  * ROT: the table is rotated (DasParams::rot_table), the term by theta (f - 1/2)
@@ -43,22 +77,65 @@ __device__ __forceinline__ float apod_cos2_p5(float w)
  * aperture edge instead of tested, so a term just outside the aperture weighs the
  * polynomial's value at the edge (|p| < 5e-7) where the reference weighs
  * cos(pi/2)^2 = 2e-15. */
-template <int INTERP, bool DEMOD, bool FASTMATH, int ROT, bool INR = false>
+template <int INTERP, bool DEMOD, bool FASTMATH, int ROT, bool INR = false, bool H = false>
 __device__ __forceinline__ void term_tail(const DasParams &p, const float4 *__restrict__ tab, float lat2, float dz2,
                                           float ka2, float dtx, float s_lim, int row, float scale, float &ax, float &ay)
 {
 	const float w    = INR ? fminf(ka2 * lat2, HALF_PI_SQ) : ka2 * lat2;
 	const float x    = __fadd_rn(lat2, dz2);
-	const float drx  = FASTMATH ? sqrt_newton(x) : __fsqrt_rn(x);
-	const float d    = __fadd_rn(dtx, drx);
-	float tt = FASTMATH ? div_rc(d, p.c, p.rc) : __fdiv_rn(d, p.c);
-	tt = __fadd_rn(tt, p.toff);
-	const float idx = __fmul_rn(tt, p.fs);
+	float idx;
+	if (H) {
+		/* precision 1: dtx carries the voxel's io = dtx fs_c + toff_fs */
+		float drx;
+		if (FASTMATH) {
+			float r;
+			asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+			drx = x * r;
+		} else {
+			drx = __fsqrt_rn(x);
+		}
+		idx = fmaf(drx, p.fs_c, dtx);
+	} else {
+		const float drx = FASTMATH ? sqrt_newton(x) : __fsqrt_rn(x);
+		const float d   = __fadd_rn(dtx, drx);
+		float tt = FASTMATH ? div_rc(d, p.c, p.rc) : __fdiv_rn(d, p.c);
+		tt = __fadd_rn(tt, p.toff);
+		idx = __fmul_rn(tt, p.fs);
+	}
 	const bool ok = INR || (idx >= 0.0f && idx < s_lim && w < HALF_PI_SQ);
-	const float a  = ok ? apod_cos2_p5(w) * scale : 0.0f;
+	const float a  = ok ? (H ? apod_cos2_p3(w) : apod_cos2_p5(w)) * scale : 0.0f;
 	const float ic = ok ? idx : 1.0f;
 	float vx, vy, f = 0.0f;
-	if (INTERP == INTERP_NEAREST && INR) {
+	if (H) {
+		/* FP16 table: index clamped to the table (nearest outside the proof may
+		 * round to the sample after the last row's end, which reads 0) */
+		if (INTERP == INTERP_NEAREST) {
+			const float r = roundf(ic);
+			const int j = row + (int)r;
+			const int last = p.C * p.T * p.S - 1;
+			const float2 v = __half22float2(__ldg((const __half2 *)tab + min(j, last)));
+			vx = INR || j <= last ? v.x : 0.0f;
+			vy = INR || j <= last ? v.y : 0.0f;
+			f = ic - r;
+		} else {
+			const int ii = (int)ic;
+			f = ic - (float)ii;
+			const __half2 f2 = __float2half2_rn(f);
+			__half2 h;
+			if (INTERP == INTERP_CUBIC) {
+				const uint4 q = __ldg((const uint4 *)tab + (unsigned)(row + ii));
+				h = __hfma2(as_half2(q.w), f2, as_half2(q.z));
+				h = __hfma2(h, f2, as_half2(q.y));
+				h = __hfma2(h, f2, as_half2(q.x));
+			} else {
+				const uint2 q = __ldg((const uint2 *)tab + (unsigned)(row + ii));
+				h = __hfma2(as_half2(q.y), f2, as_half2(q.x));
+			}
+			const float2 v = __half22float2(h);
+			vx = v.x;
+			vy = v.y;
+		}
+	} else if (INTERP == INTERP_NEAREST && INR) {
 		/* round(idx) proven inside the row: no bound check; with ROT the sample
 		 * comes pre-rotated by its phase from the table (float2 per sample) */
 		const float r = roundf(ic);
@@ -92,7 +169,7 @@ __device__ __forceinline__ void term_tail(const DasParams &p, const float4 *__re
 	}
 	if (DEMOD) {
 		float sn, cs;
-		if (ROT != 0 && (INTERP != INTERP_NEAREST || INR)) {
+		if (ROT != 0 && (INTERP != INTERP_NEAREST || INR || H)) {
 			/* table interpolation: theta (f - 1/2); nearest: theta (idx - round(idx)) */
 			float a = INTERP == INTERP_NEAREST ? __fmul_rn(p.theta, f) : fmaf(p.theta, f, -p.theta_half);
 			if (ROT == 2) {
@@ -123,6 +200,7 @@ __device__ __forceinline__ void term_tail(const DasParams &p, const float4 *__re
 struct HercVoxel {
 	float q_fix, q_var;     /* lateral coordinates fixed by r and varied by t */
 	float dz2, dtx, ka2, lim2;
+	float io;               /* precision 1: dtx fs_c + toff_fs, the index offset */
 	bool  fast;             /* every term inside the verified fast-math ranges */
 	bool  inrange;          /* every term's sample index inside [0, S - 2) (cubic), [0, S - 1) (linear), [0, S - 1/2) (nearest) */
 };
@@ -135,6 +213,7 @@ __device__ __forceinline__ HercVoxel hercules_setup(const DasParams &p, int vx, 
 	m4v(p.X, w[0], w[1], w[2], q);
 	v.dz2 = __fmul_rn(q[2], q[2]);
 	v.dtx = transmit_distance(p, w, 0);
+	v.io = fmaf(v.dtx, p.fs_c, p.toff_fs);
 	const float ka = __fdiv_rn(p.apod_scale, fabsf(q[2]));
 	v.ka2 = ka * ka;
 	v.lim2 = HALF_PI_SQ / v.ka2;
@@ -160,8 +239,13 @@ __device__ __forceinline__ HercVoxel hercules_setup(const DasParams &p, int vx, 
 	/* nearest: round(idx) <= S - 1 needs idx < S - 1/2 */
 	const float s_lim = p.interp == INTERP_CUBIC ? (float)(p.S - 2) : p.interp == INTERP_LINEAR ? (float)(p.S - 1)
 	                                                                                         : (float)p.S - 0.5f;
-	v.inrange = p.c > 0.0f && p.fs > 0.0f && imin - fabsf(imin) * 1e-4f >= 0.01f &&
-	            imax + fabsf(imax) * 1e-4f + 0.01f < s_lim;
+	/* precision 1 forms the index as sqrt(x) fs_c + io: its rounding and the
+	 * approximate reciprocal square root (relative error < 2^-22) stay below
+	 * 4e-6 of the magnitudes summed */
+	const float hm = p.half_table ? 4e-6f * (fabsf(v.io) + fabsf(p.toff_fs) + sqrtf(xmax) * 1.0001f * fabsf(p.fs_c))
+	                              : 0.0f;
+	v.inrange = p.c > 0.0f && p.fs > 0.0f && imin - fabsf(imin) * 1e-4f - hm >= 0.01f &&
+	            imax + fabsf(imax) * 1e-4f + hm + 0.01f < s_lim;
 	return v;
 }
 
@@ -170,7 +254,7 @@ __device__ __forceinline__ HercVoxel hercules_setup(const DasParams &p, int vx, 
  * column). The transmit interval is the widest of the voxels' (the deepest:
  * the aperture grows with depth); a voxel's terms outside its own interval weigh
  * exactly 0, so each voxel's sums equal its own loop's bit for bit. */
-template <int INTERP, bool DEMOD, bool FASTMATH, int ROT, int NV, bool INR = false>
+template <int INTERP, bool DEMOD, bool FASTMATH, int ROT, int NV, bool INR = false, bool H = false>
 __device__ __forceinline__ void hercules_column(const DasParams &p, const float4 *__restrict__ tab, const HercVoxel *v,
                                                 int u_begin, int u_end, float *sx, float *sy)
 {
@@ -197,8 +281,8 @@ __device__ __forceinline__ void hercules_column(const DasParams &p, const float4
 			const float lat2 = __fadd_rn(f2, __fmul_rn(dv, dv));
 			#pragma unroll
 			for (int k = 0; k < NV; k++)
-				term_tail<INTERP, DEMOD, FASTMATH, ROT, INR>(p, tab, lat2, v[k].dz2, v[k].ka2, v[k].dtx, s_lim, row, p.inv_sqrt_T,
-				                                   ax[k], ay[k]);
+				term_tail<INTERP, DEMOD, FASTMATH, ROT, INR, H>(p, tab, lat2, v[k].dz2, v[k].ka2, H ? v[k].io : v[k].dtx,
+				                                                s_lim, row, p.inv_sqrt_T, ax[k], ay[k]);
 			t_lo = 1;
 			row += p.S;
 		}
@@ -212,8 +296,8 @@ __device__ __forceinline__ void hercules_column(const DasParams &p, const float4
 			const float lat2 = __fadd_rn(f2, __fmul_rn(dv, dv));
 			#pragma unroll
 			for (int k = 0; k < NV; k++)
-				term_tail<INTERP, DEMOD, FASTMATH, ROT, INR>(p, tab, lat2, v[k].dz2, v[k].ka2, v[k].dtx, s_lim, row, 1.0f,
-				                                   ax[k], ay[k]);
+				term_tail<INTERP, DEMOD, FASTMATH, ROT, INR, H>(p, tab, lat2, v[k].dz2, v[k].ka2, H ? v[k].io : v[k].dtx,
+				                                                s_lim, row, 1.0f, ax[k], ay[k]);
 			tf += 1.0f;
 			row += p.S;
 		}
@@ -224,27 +308,27 @@ __device__ __forceinline__ void hercules_column(const DasParams &p, const float4
 
 /* One voxel on its own, with the fast or the IEEE square root and divisions (and,
  * where its sample indices are proven in range, without per-term range tests). */
-template <int INTERP>
+template <int INTERP, bool H = false>
 __device__ __forceinline__ void hercules_single(const DasParams &p, const float4 *__restrict__ tab, const HercVoxel &v,
                                              int u_begin, int u_end, float &sx, float &sy)
 {
 	const bool demod = p.fc > 0.0f;
 	const int rot = p.rot_table;
 	if (v.fast && v.inrange) {
-		if (demod && rot == 1)      hercules_column<INTERP, true, true, 1, 1, true>(p, tab, &v, u_begin, u_end, &sx, &sy);
-		else if (demod && rot == 2) hercules_column<INTERP, true, true, 2, 1, true>(p, tab, &v, u_begin, u_end, &sx, &sy);
-		else if (demod)             hercules_column<INTERP, true, true, 0, 1, true>(p, tab, &v, u_begin, u_end, &sx, &sy);
-		else                        hercules_column<INTERP, false, true, 0, 1, true>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		if (demod && rot == 1)      hercules_column<INTERP, true, true, 1, 1, true, H>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else if (demod && rot == 2) hercules_column<INTERP, true, true, 2, 1, true, H>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else if (demod)             hercules_column<INTERP, true, true, 0, 1, true, H>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else                        hercules_column<INTERP, false, true, 0, 1, true, H>(p, tab, &v, u_begin, u_end, &sx, &sy);
 	} else if (v.fast) {
-		if (demod && rot == 1)      hercules_column<INTERP, true, true, 1, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
-		else if (demod && rot == 2) hercules_column<INTERP, true, true, 2, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
-		else if (demod)             hercules_column<INTERP, true, true, 0, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
-		else                        hercules_column<INTERP, false, true, 0, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		if (demod && rot == 1)      hercules_column<INTERP, true, true, 1, 1, false, H>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else if (demod && rot == 2) hercules_column<INTERP, true, true, 2, 1, false, H>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else if (demod)             hercules_column<INTERP, true, true, 0, 1, false, H>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else                        hercules_column<INTERP, false, true, 0, 1, false, H>(p, tab, &v, u_begin, u_end, &sx, &sy);
 	} else {
-		if (demod && rot == 1)      hercules_column<INTERP, true, false, 1, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
-		else if (demod && rot == 2) hercules_column<INTERP, true, false, 2, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
-		else if (demod)             hercules_column<INTERP, true, false, 0, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
-		else                        hercules_column<INTERP, false, false, 0, 1>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		if (demod && rot == 1)      hercules_column<INTERP, true, false, 1, 1, false, H>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else if (demod && rot == 2) hercules_column<INTERP, true, false, 2, 1, false, H>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else if (demod)             hercules_column<INTERP, true, false, 0, 1, false, H>(p, tab, &v, u_begin, u_end, &sx, &sy);
+		else                        hercules_column<INTERP, false, false, 0, 1, false, H>(p, tab, &v, u_begin, u_end, &sx, &sy);
 	}
 }
 
@@ -260,7 +344,7 @@ template <int TY, int THREADS = 128> struct HercTile {
 
 /* Thread threadIdx.x of voxel tile (bx, yt, bz), outer-loop group grp: the
  * work of one das_hercules block, also run by the batched launch. */
-template <int INTERP, int TY, int THREADS = 128>
+template <int INTERP, int TY, int THREADS = 128, bool H = false>
 __device__ __forceinline__ void hercules_tile(const DasParams &p, const float4 *__restrict__ tab, int bx, int yt, int bz,
                                               int grp)
 {
@@ -295,20 +379,26 @@ __device__ __forceinline__ void hercules_tile(const DasParams &p, const float4 *
 		#pragma unroll
 		for (int k = 0; k < NV; k++) inr = inr && v[k].inrange;
 		if (inr) {
-			if (demod && rot == 1)      hercules_column<INTERP, true, true, 1, NV, true>(p, tab, v, u_begin, u_end, sx, sy);
-			else if (demod && rot == 2) hercules_column<INTERP, true, true, 2, NV, true>(p, tab, v, u_begin, u_end, sx, sy);
-			else if (demod)             hercules_column<INTERP, true, true, 0, NV, true>(p, tab, v, u_begin, u_end, sx, sy);
-			else                        hercules_column<INTERP, false, true, 0, NV, true>(p, tab, v, u_begin, u_end, sx, sy);
+			if (demod && rot == 1)      hercules_column<INTERP, true, true, 1, NV, true, H>(p, tab, v, u_begin, u_end, sx, sy);
+			else if (demod && rot == 2) hercules_column<INTERP, true, true, 2, NV, true, H>(p, tab, v, u_begin, u_end, sx, sy);
+			else if (demod)             hercules_column<INTERP, true, true, 0, NV, true, H>(p, tab, v, u_begin, u_end, sx, sy);
+			else                        hercules_column<INTERP, false, true, 0, NV, true, H>(p, tab, v, u_begin, u_end, sx, sy);
 		} else {
-			if (demod && rot == 1)      hercules_column<INTERP, true, true, 1, NV>(p, tab, v, u_begin, u_end, sx, sy);
-			else if (demod && rot == 2) hercules_column<INTERP, true, true, 2, NV>(p, tab, v, u_begin, u_end, sx, sy);
-			else if (demod)             hercules_column<INTERP, true, true, 0, NV>(p, tab, v, u_begin, u_end, sx, sy);
-			else                        hercules_column<INTERP, false, true, 0, NV>(p, tab, v, u_begin, u_end, sx, sy);
+			if (demod && rot == 1)      hercules_column<INTERP, true, true, 1, NV, false, H>(p, tab, v, u_begin, u_end, sx, sy);
+			else if (demod && rot == 2) hercules_column<INTERP, true, true, 2, NV, false, H>(p, tab, v, u_begin, u_end, sx, sy);
+			else if (demod)             hercules_column<INTERP, true, true, 0, NV, false, H>(p, tab, v, u_begin, u_end, sx, sy);
+			else                        hercules_column<INTERP, false, true, 0, NV, false, H>(p, tab, v, u_begin, u_end, sx, sy);
 		}
 	} else {
 		#pragma unroll
 		for (int k = 0; k < NV; k++)
-			if (k < nv) hercules_single<INTERP>(p, tab, v[k], u_begin, u_end, sx[k], sy[k]);
+			if (k < nv) hercules_single<INTERP, H>(p, tab, v[k], u_begin, u_end, sx[k], sy[k]);
+	}
+	if (H) {
+		/* undo the table's power-of-two scale (exact) */
+		const float us = pow2f(-half_table_shift(__ldg(p.absmax)));
+		#pragma unroll
+		for (int k = 0; k < NV; k++) { sx[k] *= us; sy[k] *= us; }
 	}
 
 	const int64_t nvox = (int64_t)p.dims[0] * p.dims[1] * p.dims[2];

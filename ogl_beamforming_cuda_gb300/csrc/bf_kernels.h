@@ -110,6 +110,14 @@ struct DasParams {
 	int32_t        rot_table;
 	uint32_t       rot_step, rot_half;
 	float          theta, theta_half;
+	/* DAS precision 1 (HERCULES fast path only): the table holds FP16 pairs of the
+	 * coefficients times 2^k, k chosen per frame from the largest channel-data
+	 * magnitude (*absmax, float bits, written by launch_das_table); the segment is
+	 * evaluated in packed FP16, the sample index is sqrt(x) * fs_c + io with io =
+	 * dtx * fs_c + toff_fs per voxel, and the voxel sums are multiplied by 2^-k */
+	int32_t        half_table;
+	unsigned      *absmax;
+	float          fs_c, toff_fs;
 };
 
 /* Exhaustively compare x * rb + correction with IEEE x / b for every float x in
@@ -134,12 +142,13 @@ cudaError_t launch_fir_tc(const void *x, uint32_t rows, uint32_t row_samples, ui
                           float2 *out, unsigned *error, cudaStream_t s);
 cudaError_t launch_das_reduce(const float2 *partial, float2 *frame, int64_t n, int groups, cudaStream_t s);
 /* HERCULES fast path (bf_das_hercules.cu): for parameters das_hercules_supported
- * accepts; `table` holds das_hercules_table_entries float4 (none for nearest) */
+ * accepts; `table` holds das_hercules_table_bytes bytes (none: nearest FP32
+ * interpolation of data that is not rotated) */
 bool        das_hercules_supported(const DasParams &p);
 /* blocks of one channel group of the HERCULES launch, and resident blocks per SM */
 int64_t     das_hercules_tiles(const DasParams &p);
 int         das_hercules_blocks_per_sm(const DasParams &p);
-int64_t     das_hercules_table_entries(const DasParams &p);
+int64_t     das_hercules_table_bytes(const DasParams &p);
 cudaError_t launch_das_hercules(const DasParams &p, float4 *table, cudaStream_t s);
 cudaError_t launch_sum(float2 *out, const float2 *const *ins, int count, float prescale, const int32_t dims[3],
                        cudaStream_t s);
@@ -150,7 +159,7 @@ cudaError_t launch_min_max(const float2 *level0, const int32_t dims[3], int mips
 enum DasBatchPath { DAS_BATCH_HERC_VOLUME = 0, DAS_BATCH_HERC_PLANE = 1, DAS_BATCH_GENERIC = 2 };
 struct DasBatchAcq {
 	DasParams     p;
-	const float4 *table;       /* HERCULES interpolation table (das_hercules_table_entries) */
+	const float4 *table;       /* HERCULES interpolation table (das_hercules_table_bytes) */
 	int32_t       path;        /* DasBatchPath */
 	int32_t       reserved;
 };

@@ -128,6 +128,10 @@ struct Context {
 	/* precision variant: 0 FP32 (reference arithmetic), 1 FP16, 2 BF16 Decode output
 	 * and tensor-core Demodulate FIR */
 	int32_t      precision = 0;
+	/* DAS precision: 0 FP32 (reference arithmetic), 1 FP16 interpolation table
+	 * (HERCULES fast path; other DAS paths stay FP32) */
+	int32_t      das_precision = 0;
+	unsigned    *d_absmax = nullptr;      /* per-frame channel-data magnitude of the FP16 table */
 	int32_t      rx_step = 1;             /* receive subsampling of HERCULES DAS (learned variant input) */
 	bool         tc_active = false;
 	void        *tc_table = nullptr;
@@ -715,6 +719,13 @@ bool fill_das_params(const Plan &pl, int kind, const void *rf, uint64_t rf_bytes
 	set_das_rotation(p);
 	p.rx_step = g.rx_step;
 	if (p.rx_step > 1 && (p.family != DAS_HERCULES || !p.fast || p.sparse_mode)) return fail(BF_LIB_ERR_KIND_UNSUPPORTED), false;
+	p.fs_c = (float)((double)p.fs / (double)p.c);
+	p.toff_fs = (float)((double)p.toff * (double)p.fs);
+	p.half_table = g.das_precision == 1 ? 1 : 0;
+	if (p.half_table) {
+		if (!g.d_absmax && !cuda_ok(cudaMalloc(&g.d_absmax, sizeof(unsigned)))) return false;
+		p.absmax = g.d_absmax;
+	}
 	return true;
 }
 
@@ -850,7 +861,7 @@ bool run_stage(int i, const void *src, uint64_t src_bytes, DeviceFrame &frame, b
 		/* OGL_BF_DAS_GENERIC=1 keeps every DAS on das_kernel (for comparisons) */
 		const char *generic = std::getenv("OGL_BF_DAS_GENERIC");
 		if (das_hercules_supported(p) && !(generic && generic[0] == '1')) {
-			const uint64_t need = (uint64_t)das_hercules_table_entries(p) * sizeof(float4);
+			const uint64_t need = (uint64_t)das_hercules_table_bytes(p);
 			if (need > g.das_table_bytes) {
 				cudaStreamSynchronize(g.stream);
 				cudaFree(g.das_table);
@@ -1150,7 +1161,7 @@ cudaError_t batch_launch(cudaStream_t s)
 			if (e != cudaSuccess) return e;
 			last = out_idx;
 		}
-		if (a.path != DAS_BATCH_GENERIC && das_hercules_table_entries(a.das) > 0) {
+		if (a.path != DAS_BATCH_GENERIC && das_hercules_table_bytes(a.das) > 0) {
 			const cudaError_t e = launch_das_table(a.das, a.das_table, s);
 			if (e != cudaSuccess) return e;
 		}
@@ -1259,8 +1270,8 @@ bool build_batch(const BeamformerParameters *params, uint32_t count, const void 
 		if (a.das.family == DAS_HERCULES && das_hercules_supported(a.das)) {
 			a.path = DAS_BATCH_HERC_PLANE;
 			any_volume = any_volume || a.das.dims[1] >= 4;
-			const uint64_t n = (uint64_t)das_hercules_table_entries(a.das);
-			if (n && !cuda_ok(cudaMalloc(&a.das_table, n * sizeof(float4)))) return false;
+			const uint64_t n = (uint64_t)das_hercules_table_bytes(a.das);
+			if (n && !cuda_ok(cudaMalloc(&a.das_table, n))) return false;
 		} else if (a.das.family == DAS_FORCES && !a.das.sparse_mode) {
 			a.path = DAS_BATCH_GENERIC;
 		} else {
@@ -1639,6 +1650,16 @@ LIB_FN uint32_t beamformer_gb300_set_filter_precision(int32_t precision)
 	return 1;
 }
 
+LIB_FN uint32_t beamformer_gb300_set_das_precision(int32_t precision)
+{
+	if (precision < 0 || precision > 1) return fail(BF_LIB_ERR_KIND_UNSUPPORTED);
+	if (precision != g.das_precision) {
+		g.das_precision = precision;
+		g.dirty = true;
+	}
+	return 1;
+}
+
 LIB_FN uint32_t beamformer_gb300_set_interpolation(int32_t mode)
 {
 	if (mode < -1 || mode > 2) return fail(BF_LIB_ERR_KIND_UNSUPPORTED);
@@ -1752,6 +1773,7 @@ LIB_FN void beamformer_gb300_shutdown(void)
 	cudaFree(g.hadamard);
 	cudaFree(g.das_partial);
 	cudaFree(g.das_table);
+	cudaFree(g.d_absmax);
 	cudaFree(g.tc_table);
 	cudaFree(g.d_tc_error);
 	cudaFree(g.d_mismatch);
@@ -1774,6 +1796,7 @@ LIB_FN void beamformer_gb300_shutdown(void)
 	fresh.timeout_ms = g.timeout_ms;
 	fresh.interpolation_override = g.interpolation_override;
 	fresh.precision = g.precision;
+	fresh.das_precision = g.das_precision;
 	fresh.rx_step = g.rx_step;
 	g = fresh;
 }
@@ -1785,7 +1808,7 @@ LIB_FN uint32_t beamformer_gb300_beamform_batch(const BeamformerParameters *para
 {
 	if (!parameters || !rf || !rf_size || !out || count == 0) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
 	if (g.shader_count <= 0) return fail(BF_LIB_ERR_KIND_INVALID_COMPUTE_STAGE);
-	if (g.precision != 0) return fail(BF_LIB_ERR_KIND_UNSUPPORTED);
+	if (g.precision != 0 || g.das_precision != 0) return fail(BF_LIB_ERR_KIND_UNSUPPORTED);
 	for (uint32_t i = 0; i < count; i++)
 		if (!rf[i] || !out[i]) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
 	if (!ensure_cuda()) return 0;

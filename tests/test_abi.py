@@ -200,3 +200,8 @@ def test_filter_precision_argument_checks(lib):
     assert lib.beamformer_gb300_set_filter_precision(-1) == 0
     for p in (1, 2, 0):
         assert lib.beamformer_gb300_set_filter_precision(p) == 1
+    assert lib.beamformer_gb300_set_das_precision(2) == 0
+    assert lib.beamformer_get_last_error() == abi.ERR["UNSUPPORTED"]
+    assert lib.beamformer_gb300_set_das_precision(-1) == 0
+    for p in (1, 0):
+        assert lib.beamformer_gb300_set_das_precision(p) == 1

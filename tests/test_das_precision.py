@@ -1,0 +1,107 @@
+"""DAS precision 1: the HERCULES interpolation table in FP16 (coefficients scaled
+by a power of two from the frame's largest channel-data magnitude, segments
+evaluated in packed FP16), the sample index from an approximate square root and
+one FMA, a degree-3 apodization; FP32 sums. Checked against the oracle (the
+reference's FP32 arithmetic) on identical seeded int16 RF, for every
+interpolation, plane and volume tiles, both demodulation phase paths
+(theta = 2 pi and 4 pi), data without demodulation, voxels outside the in-range
+proof and input amplitudes far from full scale.
+
+Bound: NRMSE <= -50 dB against the oracle (the mixed-precision metric allows
+-40 dB; FP16 keeps 11 significant bits of each coefficient)."""
+import numpy as np
+import pytest
+
+from ogl_beamforming_cuda_gb300 import abi
+from ogl_beamforming_cuda_gb300.client import Beamformer, BeamformerError
+from bf_cases import small_params, small_raw, oracle_for, nrmse
+
+pytestmark = pytest.mark.gpu
+SH = abi.SHADER
+KAISER = (5.65, 5e6, 25e6, 32)
+BOUND_DB = -50.0
+
+
+@pytest.fixture(autouse=True)
+def fp32_afterwards():
+    yield
+    Beamformer().lib.beamformer_gb300_set_das_precision(0)
+
+
+def half_vs_oracle(bp, pipe, raw, interp, kaiser=KAISER):
+    bf = Beamformer().configure(bp, pipe, kaiser=kaiser, interpolation=interp)
+    assert bf.lib.beamformer_gb300_set_das_precision(1)
+    bf.push(raw)
+    bf.synchronize()
+    vol = bf.frame(0)[0].copy()
+    orc = oracle_for(bf, bp, pipe, kaiser=kaiser)
+    orc.interpolation = interp
+    ref = orc.compute(raw)["frame"]
+    assert np.all(np.isfinite(vol))
+    return nrmse(vol, ref), vol, ref
+
+
+@pytest.mark.parametrize("interp", (0, 1, 2))
+@pytest.mark.parametrize("points", ((48, 1, 64), (16, 8, 32)))
+@pytest.mark.parametrize("fc_scale", (1.0, 2.0))
+def test_half_table_against_oracle(interp, points, fc_scale):
+    bp = small_params(S=2048, C=16, T=16, points=points, D=2)
+    bp.center_frequency *= fc_scale
+    raw = small_raw(bp, n_points=12, n_speckle=300)
+    db, _, _ = half_vs_oracle(bp, [SH["Decode"], SH["Demodulate"], SH["DASFast"]], raw, interp)
+    print(f"interp={interp} points={points} fc x {fc_scale}: {db:.1f} dB")
+    assert db <= BOUND_DB, db
+
+
+@pytest.mark.parametrize("interp", (0, 1, 2))
+def test_half_table_without_demodulation(interp):
+    bp = small_params(S=512, C=16, T=16, points=(16, 4, 24), D=1)
+    raw = small_raw(bp)
+    db, _, _ = half_vs_oracle(bp, [SH["Decode"], SH["DASFast"]], raw, interp, kaiser=None)
+    assert db <= BOUND_DB, db
+
+
+@pytest.mark.parametrize("interp", (0, 1, 2))
+def test_half_table_outside_the_proof(interp):
+    """Voxels from the array plane (depth 0: the IEEE square root) to beyond the
+    last sample (per-term range tests, nearest indices clamped to the table)."""
+    bp = small_params(S=512, C=16, T=16, points=(12, 4, 40), D=2)
+    bp.output_min_coordinate[2] = 0.0
+    bp.output_max_coordinate[2] = 12e-3
+    raw = small_raw(bp, n_points=10, n_speckle=200)
+    db, vol, ref = half_vs_oracle(bp, [SH["Decode"], SH["Demodulate"], SH["DASFast"]], raw, interp)
+    assert db <= BOUND_DB, db
+
+
+@pytest.mark.parametrize("shift", (0, 7, 12))
+def test_half_table_scale_follows_the_data(shift):
+    """Quiet input (amplitudes divided by 2^shift, down to a few LSB): the
+    power-of-two table scale keeps the FP16 coefficients in their normal range."""
+    bp = small_params(S=1024, C=16, T=16, points=(16, 4, 32), D=2)
+    raw = small_raw(bp, n_points=12, n_speckle=300)
+    raw = (raw.astype(np.int32) >> shift).astype(np.int16)
+    db, _, _ = half_vs_oracle(bp, [SH["Decode"], SH["Demodulate"], SH["DASFast"]], raw, 1)
+    assert db <= BOUND_DB, db
+
+
+def test_half_table_zero_input_is_zero():
+    bp = small_params(S=512, C=16, T=16, points=(16, 4, 16), D=2)
+    raw = np.zeros_like(small_raw(bp))
+    bf = Beamformer().configure(bp, [SH["Decode"], SH["Demodulate"], SH["DASFast"]], kaiser=KAISER, interpolation=1)
+    assert bf.lib.beamformer_gb300_set_das_precision(1)
+    bf.push(raw)
+    bf.synchronize()
+    assert not np.any(bf.frame(0)[0])
+
+
+def test_batch_refuses_half_table():
+    import torch
+    bp = small_params(S=256, C=16, T=16, points=(8, 4, 8))
+    raw = torch.from_numpy(small_raw(bp)).cuda()
+    out = torch.zeros(2 * 8 * 4 * 8, dtype=torch.float32, device="cuda")
+    pipe = [SH["Decode"], SH["Demodulate"], SH["DAS"]]
+    bf = Beamformer().configure(bp, pipe, kaiser=KAISER)
+    assert bf.lib.beamformer_gb300_set_das_precision(1)
+    with pytest.raises(BeamformerError):
+        bf.beamform_batch([bp], [raw.data_ptr()], [raw.numel() * 2], [out.data_ptr()])
+    assert bf.lib.beamformer_get_last_error() == abi.ERR["UNSUPPORTED"]
