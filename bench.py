@@ -55,6 +55,8 @@ def parse():
                     help="only push this many copies of one device-resident frame through the pipeline "
                          "(for a profiler), print per-stage ms and exit")
     ap.add_argument("--points", default=",".join(map(str, POINTS)), help="voxel grid for --profile-frames")
+    ap.add_argument("--precision", type=int, default=0, choices=[0, 1],
+                    help="for --profile-frames: 1 runs the mixed pipeline (FP16 front end, FP16 DAS table)")
     ap.add_argument("--variant", default="plain", choices=["plain", "precision", "batched", "learned"],
                     help="plain: the 3D pipeline (default, the headline line); precision: the FP16/BF16 front end "
                          "on the 4096-sample plane; batched: 32 mixed acquisitions in one call; learned: every-4th-"
@@ -80,12 +82,14 @@ def profile_frames(args):
     points = tuple(int(v) for v in args.points.split(","))
     bp, pipe, kaiser = workload(points)
     bf = Beamformer().configure(bp, pipe, kaiser=kaiser)
+    assert bf.lib.beamformer_gb300_set_filter_precision(args.precision)
+    assert bf.lib.beamformer_gb300_set_das_precision(args.precision)
     raw = torch.from_numpy(synth.acquisition(bp, 1000, n_points=N_POINTS, n_speckle=args.speckle, device="cuda:0"))
     raw = raw.to("cuda:0")
     for _ in range(args.profile_frames):
         bf.push_device(raw.data_ptr(), raw.numel() * 2)
     bf.synchronize()
-    print(json.dumps({"points": points, "frames": args.profile_frames,
+    print(json.dumps({"points": points, "frames": args.profile_frames, "precision": args.precision,
                       "stage_ms": {k: v * 1e3 for k, v in stage_times(bf, args.profile_frames).items()}}))
     return 0
 
@@ -295,7 +299,41 @@ def run_ours(args, rank, world, local, dist):
         tt = torch.tensor([t, te], device=f"cuda:{local}")
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t, te = float(tt[0]), float(tt[1])
-    return dict(t=t, te=te, stages=stages, launches=launches, clocks=clk.summary(), nbytes=nbytes, out_bytes=8 * vox)
+
+    # the same workload through the mixed pipeline (FP16 decode output and
+    # tensor-core FIR, FP16 DAS table, FP32 sums): device-resident and end-to-end
+    # volumes/s, and its output volume against the FP32 output volume
+    mixed = None
+    if rank == 0:
+        ref_vol = out.numpy().astype(np.float64)
+        assert L.beamformer_gb300_set_filter_precision(1) and L.beamformer_gb300_set_das_precision(1)
+        dev = host.to(f"cuda:{local}")
+
+        def mstep():
+            for f in range(FRAMES):
+                bf.push_device(dev[f].data_ptr(), nbytes)
+        for _ in range(max(args.warmup, 3)):
+            mstep()
+        bf.synchronize()
+        m_ms = _events_ms(mstep, stream, max(args.steps, 1))
+        m_stages = stage_times(bf, FRAMES)
+        del dev
+        e2e_step()
+        torch.cuda.synchronize()
+        h0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        m_te = (time.perf_counter() - h0) / max(args.steps, 1)
+        m_vol = out.numpy().astype(np.float64)
+        assert L.beamformer_gb300_set_filter_precision(0) and L.beamformer_gb300_set_das_precision(0)
+        db = float(20 * np.log10(np.sqrt(np.mean((m_vol - ref_vol) ** 2) / np.mean(ref_vol ** 2))))
+        mixed = {"value": 1e3 / m_ms, "unit": "volumes/s", "e2e": 1.0 / m_te if args.steps else None,
+                 "das_ms": (m_stages.get("DASFast") or 0.0) * 1e3,
+                 "nrmse_db_vs_fp32_volume": db, "bound_db": -40.0,
+                 "arithmetic": "FP16 decode output + tcgen05 FIR, FP16 DAS interpolation table, FP32 sums"}
+    return dict(t=t, te=te, stages=stages, launches=launches, clocks=clk.summary(), nbytes=nbytes, out_bytes=8 * vox,
+                mixed=mixed)
 
 
 def cpu_sample(budget_s=12.0):
@@ -713,6 +751,10 @@ def main():
         "stages": stage_roof,
         "clocks": r["clocks"],
     }
+    if r.get("mixed"):
+        m = dict(r["mixed"])
+        m["speedup_vs_fp32"] = m["value"] / (value / world)     # rank 0 alone runs the mixed pipeline
+        line["mixed_precision"] = m
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample()
     print(json.dumps(line))
