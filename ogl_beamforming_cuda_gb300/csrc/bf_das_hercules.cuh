@@ -306,6 +306,123 @@ __device__ __forceinline__ void hercules_column(const DasParams &p, const float4
 	}
 }
 
+/* Precision 1: sample value of one term from the FP16 table at index ic (proven
+ * in range), and the fraction the phase rotation needs. */
+template <int INTERP>
+__device__ __forceinline__ void sample_half(const float4 *__restrict__ tab, int row, float ic, float &f, float &vx,
+                                            float &vy)
+{
+	float2 v;
+	if (INTERP == INTERP_NEAREST) {
+		const float r = roundf(ic);
+		v = __half22float2(__ldg((const __half2 *)tab + (row + (int)r)));
+		f = ic - r;
+	} else {
+		const int ii = (int)ic;
+		f = ic - (float)ii;
+		const __half2 f2 = __float2half2_rn(f);
+		__half2 h;
+		if (INTERP == INTERP_CUBIC) {
+			const uint4 q = __ldg((const uint4 *)tab + (unsigned)(row + ii));
+			h = __hfma2(as_half2(q.w), f2, as_half2(q.z));
+			h = __hfma2(h, f2, as_half2(q.y));
+			h = __hfma2(h, f2, as_half2(q.x));
+		} else {
+			const uint2 q = __ldg((const uint2 *)tab + (unsigned)(row + ii));
+			h = __hfma2(as_half2(q.y), f2, as_half2(q.x));
+		}
+		v = __half22float2(h);
+	}
+	vx = v.x;
+	vy = v.y;
+}
+
+/* Precision 1, one transmit of two depths of a column (the float2 lanes are the
+ * two voxels) whose sample indices are proven in range: the per-voxel arithmetic
+ * of term_tail<..., INR, H> in packed FP32 (per component the same IEEE
+ * operations as the scalar forms). ROT != 0 or !DEMOD. */
+template <int INTERP, bool DEMOD, int ROT>
+__device__ __forceinline__ void term_h2(const DasParams &p, const float4 *__restrict__ tab, float lat2, float2 dz2,
+                                        float2 ka2, float2 io, int row, float scale, float2 &ax, float2 &ay)
+{
+	const float2 l2 = make_float2(lat2, lat2);
+	float2 w = __fmul2_rn(ka2, l2);
+	w.x = fminf(w.x, HALF_PI_SQ);
+	w.y = fminf(w.y, HALF_PI_SQ);
+	const float2 x = __fadd2_rn(l2, dz2);
+	float r0, r1;
+	asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(x.x));
+	asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r1) : "f"(x.y));
+	const float2 idx = __ffma2_rn(__fmul2_rn(x, make_float2(r0, r1)), make_float2(p.fs_c, p.fs_c), io);
+	/* apod_cos2_p3 on both voxels */
+	float2 a = __ffma2_rn(make_float2(-0.031044068f, -0.031044068f), w, make_float2(0.31450406f, 0.31450406f));
+	a = __ffma2_rn(a, w, make_float2(-0.99229395f, -0.99229395f));
+	a = __ffma2_rn(a, w, make_float2(1.0f, 1.0f));
+	if (scale != 1.0f) a = __fmul2_rn(a, make_float2(scale, scale));
+	float2 f, vx, vy;
+	sample_half<INTERP>(tab, row, idx.x, f.x, vx.x, vy.x);
+	sample_half<INTERP>(tab, row, idx.y, f.y, vx.y, vy.y);
+	if (DEMOD) {
+		float2 ang = INTERP == INTERP_NEAREST ? __fmul2_rn(make_float2(p.theta, p.theta), f)
+		                                      : __ffma2_rn(make_float2(p.theta, p.theta), f,
+		                                                   make_float2(-p.theta_half, -p.theta_half));
+		if (ROT == 2) {
+			const float2 k = make_float2(-rintf(ang.x * 0.159154943f), -rintf(ang.y * 0.159154943f));
+			ang = __ffma2_rn(k, make_float2(6.28125f, 6.28125f), ang);
+			ang = __ffma2_rn(k, make_float2(0x1.fb5444p-10f, 0x1.fb5444p-10f), ang);
+		}
+		float2 sn, cs;
+		__sincosf(ang.x, &sn.x, &cs.x);
+		__sincosf(ang.y, &sn.y, &cs.y);
+		const float2 ca = __fmul2_rn(a, cs), sa = __fmul2_rn(a, sn);
+		ax = __ffma2_rn(ca, vx, __ffma2_rn(make_float2(-sa.x, -sa.y), vy, ax));
+		ay = __ffma2_rn(sa, vx, __ffma2_rn(ca, vy, ay));
+	} else {
+		ax = __ffma2_rn(a, vx, ax);
+		ay = __ffma2_rn(a, vy, ay);
+	}
+}
+
+/* Precision 1, NV = 2 voxels proven in range: hercules_column with term_h2; the
+ * lateral offset of a transmit is one FMA (q - t pitch) and its square plus the
+ * fixed offset's another. */
+template <int INTERP, bool DEMOD, int ROT>
+__device__ __forceinline__ void hercules_column_h2(const DasParams &p, const float4 *__restrict__ tab, const HercVoxel *v,
+                                                   int u_begin, int u_end, float *sx, float *sy)
+{
+	const float pitch_fix = p.rx_cols ? p.px : p.py, pitch_var = p.rx_cols ? p.py : p.px;
+	const float q_fix = v[0].q_fix, q_var = v[0].q_var;
+	const float lim2 = fmaxf(v[0].lim2, v[1].lim2);
+	const float2 dz2 = make_float2(v[0].dz2, v[1].dz2), ka2 = make_float2(v[0].ka2, v[1].ka2);
+	const float2 io = make_float2(v[0].io, v[1].io);
+	for (int r = u_begin; r < u_end; r += p.rx_step) {
+		const float df = fmaf(-(float)r, pitch_fix, q_fix);
+		const float f2 = df * df;
+		int t_lo, t_hi;
+		aperture_interval(q_var, pitch_var, lim2 - f2, p.T, t_lo, t_hi);
+		if (t_lo > t_hi) continue;
+		float2 ax = make_float2(0.0f, 0.0f), ay = make_float2(0.0f, 0.0f);
+		int row = (r * p.T + t_lo) * p.S;
+		if (t_lo == 0) {
+			term_h2<INTERP, DEMOD, ROT>(p, tab, fmaf(q_var, q_var, f2), dz2, ka2, io, row, p.inv_sqrt_T, ax, ay);
+			t_lo = 1;
+			row += p.S;
+		}
+		float tf = (float)t_lo;
+		#pragma unroll 2
+		for (int t = t_lo; t <= t_hi; t++) {
+			const float dv = fmaf(-tf, pitch_var, q_var);
+			term_h2<INTERP, DEMOD, ROT>(p, tab, fmaf(dv, dv, f2), dz2, ka2, io, row, 1.0f, ax, ay);
+			tf += 1.0f;
+			row += p.S;
+		}
+		sx[0] += ax.x;
+		sx[1] += ax.y;
+		sy[0] += ay.x;
+		sy[1] += ay.y;
+	}
+}
+
 /* One voxel on its own, with the fast or the IEEE square root and divisions (and,
  * where its sample indices are proven in range, without per-term range tests). */
 template <int INTERP, bool H = false>
@@ -378,7 +495,11 @@ __device__ __forceinline__ void hercules_tile(const DasParams &p, const float4 *
 		bool inr = true;
 		#pragma unroll
 		for (int k = 0; k < NV; k++) inr = inr && v[k].inrange;
-		if (inr) {
+		if (H && NV == 2 && inr && (rot != 0 || !demod)) {
+			if (demod && rot == 1)      hercules_column_h2<INTERP, true, 1>(p, tab, v, u_begin, u_end, sx, sy);
+			else if (demod)             hercules_column_h2<INTERP, true, 2>(p, tab, v, u_begin, u_end, sx, sy);
+			else                        hercules_column_h2<INTERP, false, 0>(p, tab, v, u_begin, u_end, sx, sy);
+		} else if (inr) {
 			if (demod && rot == 1)      hercules_column<INTERP, true, true, 1, NV, true, H>(p, tab, v, u_begin, u_end, sx, sy);
 			else if (demod && rot == 2) hercules_column<INTERP, true, true, 2, NV, true, H>(p, tab, v, u_begin, u_end, sx, sy);
 			else if (demod)             hercules_column<INTERP, true, true, 0, NV, true, H>(p, tab, v, u_begin, u_end, sx, sy);
