@@ -351,8 +351,9 @@ LIB_FN uint32_t beamformer_gb300_set_filter_precision(int32_t precision);
  * FP16), the sample index from an approximate square root and one FMA, and a
  * degree-3 apodization polynomial, with FP32 sums. Applies where DAS runs on the
  * HERCULES fast path (DASFast; dense channel data, no sparse elements, no
- * coherency weighting); other DAS stages stay FP32. beamformer_gb300_beamform_batch
- * fails with UNSUPPORTED while 1 is selected. Takes effect at the next compute. */
+ * coherency weighting; in beamformer_gb300_beamform_batch its HERCULES
+ * acquisitions, each table with its own scale); other DAS stages stay FP32.
+ * Takes effect at the next compute. */
 LIB_FN uint32_t beamformer_gb300_set_das_precision(int32_t precision);
 
 /* Receive-aperture subsampling of HERCULES delay-and-sum (no counterpart in the

@@ -24,10 +24,11 @@
 
 namespace bf {
 
-/* GENERAL = false: HERCULES tiles (up to 80 registers, 6 CTAs per SM); true:
- * tiles of the general path (FORCES), compiled on their own (64 registers, 8
- * CTAs per SM) with their parameters copied to registers per tile. */
-template <int INTERP, bool GENERAL>
+/* GENERAL = false: HERCULES tiles (up to 80 registers, 6 CTAs per SM), from the
+ * FP32 table or, with H (DAS precision 1), the FP16 table; true: tiles of the
+ * general path (FORCES), compiled on their own (64 registers, 8 CTAs per SM)
+ * with their parameters copied to registers per tile. */
+template <int INTERP, bool GENERAL, bool H = false>
 __global__ void __launch_bounds__(DAS_THREADS, GENERAL ? 8 : 6)
 das_batch(const __grid_constant__ DasBatchArgs args, const int4 *__restrict__ items, int n_items, int *next)
 {
@@ -41,8 +42,8 @@ das_batch(const __grid_constant__ DasBatchArgs args, const int4 *__restrict__ it
 		const int4 w = __ldg(items + it);
 		const DasBatchAcq &a = args.acq[w.x];
 		if (!GENERAL) {
-			if (a.path == DAS_BATCH_HERC_VOLUME) hercules_tile<INTERP, 4>(a.p, a.table, w.y, w.z, w.w, 0);
-			else                                 hercules_tile<INTERP, 1>(a.p, a.table, w.y, w.z, w.w, 0);
+			if (a.path == DAS_BATCH_HERC_VOLUME) hercules_tile<INTERP, 4, DAS_THREADS, H>(a.p, a.table, w.y, w.z, w.w, 0);
+			else                                 hercules_tile<INTERP, 1, DAS_THREADS, H>(a.p, a.table, w.y, w.z, w.w, 0);
 		} else {
 			const int vx = w.y * DAS_TX + (int)(threadIdx.x & (DAS_TX - 1));
 			const int vz = w.w * DAS_TZ + (int)(threadIdx.x / DAS_TX);
@@ -77,7 +78,7 @@ void das_batch_tiles(const DasParams &p, int path, int tiles[3])
 }
 
 cudaError_t launch_das_batch(const DasBatchArgs &args, const int4 *items, int n_items, int *counter, int interp,
-                             bool general, int ctas, cudaStream_t s)
+                             bool general, bool half, int ctas, cudaStream_t s)
 {
 	if (n_items <= 0) return cudaSuccess;
 	for (int i = 0; i < DAS_BATCH_MAX; i++)
@@ -85,6 +86,7 @@ cudaError_t launch_das_batch(const DasBatchArgs &args, const int4 *items, int n_
 	cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), s);
 	if (e != cudaSuccess) return e;
 #define BF_BATCH(I) (general ? das_batch<I, true><<<ctas, DAS_THREADS, 0, s>>>(args, items, n_items, counter) \
+                     : half  ? das_batch<I, false, true><<<ctas, DAS_THREADS, 0, s>>>(args, items, n_items, counter) \
                              : das_batch<I, false><<<ctas, DAS_THREADS, 0, s>>>(args, items, n_items, counter))
 	switch (interp) {
 	case INTERP_CUBIC:  BF_BATCH(INTERP_CUBIC); break;

@@ -172,7 +172,7 @@ struct DasBatchArgs {
 /* tile grid of an acquisition on a path; work items are int4 (acquisition, tile x, y, z) */
 void        das_batch_tiles(const DasParams &p, int path, int tiles[3]);
 cudaError_t launch_das_batch(const DasBatchArgs &args, const int4 *items, int n_items, int *counter, int interp,
-                             bool general, int ctas, cudaStream_t s);
+                             bool general, bool half, int ctas, cudaStream_t s);
 /* the per-frame HERCULES interpolation table alone (cubic / linear; nothing for nearest) */
 cudaError_t launch_das_table(const DasParams &p, float4 *table, cudaStream_t s);
 

@@ -1044,6 +1044,7 @@ struct BatchAcqState {
 	uint64_t    chan_bytes = 0;
 	StageTables tables[MAX_COMPUTE_SHADER_STAGES];
 	float4     *das_table = nullptr;
+	unsigned   *absmax = nullptr;       /* FP16 table scale (DAS precision 1) */
 	int8_t     *hadamard = nullptr;
 	int32_t     sylvester = 0, base = 0;
 	float       M[16] = {};
@@ -1068,6 +1069,7 @@ struct BatchState {
 	std::vector<BatchAcqState> acq;
 	std::vector<BatchChunk>    chunks;
 	int                        interp = INTERP_NEAREST;
+	bool                       half = false;          /* FP16 tables (DAS precision 1) */
 	int                        ctas = 0;             /* persistent CTAs of the HERCULES launch */
 	int                        ctas_general = 0;     /* and of the general-path launch */
 	bool                       volume_tiles = true;
@@ -1086,6 +1088,7 @@ void free_batch()
 		cudaFree(a.chan[1]);
 		for (auto &t : a.tables) { cudaFree(t.taps); cudaFree(t.phasor); }
 		cudaFree(a.das_table);
+		cudaFree(a.absmax);
 		cudaFree(a.hadamard);
 	}
 	for (auto &c : gb.chunks) {
@@ -1121,6 +1124,8 @@ uint64_t batch_signature(const BeamformerParameters *params, uint32_t count, con
 	h = fnv1a(h, g.sparse_elements, sizeof(g.sparse_elements));
 	h = fnv1a(h, g.focal_vectors, sizeof(g.focal_vectors));
 	h = fnv1a(h, &g.interpolation_override, sizeof(g.interpolation_override));
+	h = fnv1a(h, &g.das_precision, sizeof(g.das_precision));
+	h = fnv1a(h, &g.rx_step, sizeof(g.rx_step));
 	return h;
 }
 
@@ -1128,9 +1133,11 @@ uint64_t batch_signature(const BeamformerParameters *params, uint32_t count, con
 cudaError_t batch_das(cudaStream_t s)
 {
 	for (auto &c : gb.chunks) {
-		cudaError_t e = launch_das_batch(*c.args, c.d_items[0], c.n_items[0], c.d_counter, gb.interp, false, gb.ctas, s);
+		cudaError_t e = launch_das_batch(*c.args, c.d_items[0], c.n_items[0], c.d_counter, gb.interp, false, gb.half,
+		                                 gb.ctas, s);
 		if (e != cudaSuccess) return e;
-		e = launch_das_batch(*c.args, c.d_items[1], c.n_items[1], c.d_counter + 1, gb.interp, true, gb.ctas_general, s);
+		e = launch_das_batch(*c.args, c.d_items[1], c.n_items[1], c.d_counter + 1, gb.interp, true, false,
+		                     gb.ctas_general, s);
 		if (e != cudaSuccess) return e;
 	}
 	return cudaSuccess;
@@ -1272,6 +1279,12 @@ bool build_batch(const BeamformerParameters *params, uint32_t count, const void 
 			any_volume = any_volume || a.das.dims[1] >= 4;
 			const uint64_t n = (uint64_t)das_hercules_table_bytes(a.das);
 			if (n && !cuda_ok(cudaMalloc(&a.das_table, n))) return false;
+			if (a.das.half_table) {
+				/* each acquisition's table has its own scale */
+				if (!cuda_ok(cudaMalloc(&a.absmax, sizeof(unsigned)))) return false;
+				a.das.absmax = a.absmax;
+				gb.half = true;
+			}
 		} else if (a.das.family == DAS_FORCES && !a.das.sparse_mode) {
 			a.path = DAS_BATCH_GENERIC;
 		} else {
@@ -1808,7 +1821,7 @@ LIB_FN uint32_t beamformer_gb300_beamform_batch(const BeamformerParameters *para
 {
 	if (!parameters || !rf || !rf_size || !out || count == 0) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
 	if (g.shader_count <= 0) return fail(BF_LIB_ERR_KIND_INVALID_COMPUTE_STAGE);
-	if (g.precision != 0 || g.das_precision != 0) return fail(BF_LIB_ERR_KIND_UNSUPPORTED);
+	if (g.precision != 0) return fail(BF_LIB_ERR_KIND_UNSUPPORTED);
 	for (uint32_t i = 0; i < count; i++)
 		if (!rf[i] || !out[i]) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
 	if (!ensure_cuda()) return 0;

@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from ogl_beamforming_cuda_gb300 import abi
-from ogl_beamforming_cuda_gb300.client import Beamformer, BeamformerError
+from ogl_beamforming_cuda_gb300.client import Beamformer
 from bf_cases import small_params, small_raw, oracle_for, nrmse
 
 pytestmark = pytest.mark.gpu
@@ -94,14 +94,17 @@ def test_half_table_zero_input_is_zero():
     assert not np.any(bf.frame(0)[0])
 
 
-def test_batch_refuses_half_table():
-    import torch
-    bp = small_params(S=256, C=16, T=16, points=(8, 4, 8))
-    raw = torch.from_numpy(small_raw(bp)).cuda()
-    out = torch.zeros(2 * 8 * 4 * 8, dtype=torch.float32, device="cuda")
-    pipe = [SH["Decode"], SH["Demodulate"], SH["DAS"]]
-    bf = Beamformer().configure(bp, pipe, kaiser=KAISER)
+@pytest.mark.parametrize("interp", (0, 1))
+def test_batch_with_half_table(interp):
+    """The batched variant with FP16 tables, each acquisition with its own scale:
+    every volume against the oracle (FORCES acquisitions keep the FP32 path)."""
+    from test_batch import make_batch, PIPE
+    params, raws, rf, out = make_batch(40)
+    bf = Beamformer().configure(params[0], PIPE, kaiser=KAISER, interpolation=interp)
     assert bf.lib.beamformer_gb300_set_das_precision(1)
-    with pytest.raises(BeamformerError):
-        bf.beamform_batch([bp], [raw.data_ptr()], [raw.numel() * 2], [out.data_ptr()])
-    assert bf.lib.beamformer_get_last_error() == abi.ERR["UNSUPPORTED"]
+    bf.beamform_batch(params, [t.data_ptr() for t in rf], [t.numel() * 2 for t in rf], [t.data_ptr() for t in out])
+    for i, (bp, raw) in enumerate(zip(params, raws)):
+        orc = oracle_for(bf, bp, PIPE, kaiser=KAISER)
+        orc.interpolation = interp
+        db = nrmse(out[i].cpu().numpy(), orc.compute(raw)["frame"])
+        assert db <= BOUND_DB, (i, db)
