@@ -64,6 +64,16 @@ class Beamformer:
         self._check(L.beamformer_gb300_set_interpolation(interpolation), "interpolation")
         return self
 
+    def set_precision(self, filter=None, das=None):
+        """Arithmetic of the front end (0 FP32, 1 FP16, 2 BF16 Decode output with the
+        tensor-core FIR) and of HERCULES DAS (0 FP32, 1 FP16 interpolation table);
+        None leaves that one as it is. Both persist in the library until changed."""
+        if filter is not None:
+            self._check(self.lib.beamformer_gb300_set_filter_precision(int(filter)), "filter precision")
+        if das is not None:
+            self._check(self.lib.beamformer_gb300_set_das_precision(int(das)), "DAS precision")
+        return self
+
     # ---- compute ----
     def beamform(self, raw, timeout_ms=-1):
         """beamform_data_synchronized: push host RF, compute, return the output volume."""

@@ -225,15 +225,16 @@ def driver_setup(zbp, output_points=(512, 1, 1024), lateral=(-60e-3, 60e-3), axi
             "focal_vectors": focal_vectors(zbp), "sparse_elements": sparse}
 
 
-def throughput(base, study, frame=0, loops=16, **extent):
+def throughput(base, study, frame=0, loops=16, das_precision=0, **extent):
     """Frame time and RF throughput of one study frame pushed `loops` times
     through the library with the reference driver's configuration (its looping
-    mode, tests/throughput.c:384-404)."""
+    mode, tests/throughput.c:384-404); das_precision 1 beamforms HERCULES
+    studies from the FP16 interpolation table."""
     from .client import Beamformer
     st = Study(base, study)
     cfg = driver_setup(st.zbp, **extent)
     bp, pipeline = cfg.pop("bp"), cfg.pop("pipeline")
-    bf = Beamformer().configure(bp, pipeline, **cfg)
+    bf = Beamformer().configure(bp, pipeline, **cfg).set_precision(das=das_precision)
     data = st.frame(frame)
     size = int(bp.rf_raw_dim[0]) * int(bp.rf_raw_dim[1]) * 2
     if data.nbytes < size:
@@ -246,8 +247,10 @@ def throughput(base, study, frame=0, loops=16, **extent):
         bf.push(data)
     bf.synchronize()
     dt = (time.perf_counter() - t0) / loops
+    bf.set_precision(das=0)
     return {"study": study, "frame": frame, "frames": loops, "ms_per_frame": dt * 1e3,
-            "rf_gb_per_s": size / dt / 1e9, "output_points": [int(v) for v in bp.output_points[:3]]}
+            "rf_gb_per_s": size / dt / 1e9, "output_points": [int(v) for v in bp.output_points[:3]],
+            "das_precision": das_precision}
 
 
 def main():
@@ -256,8 +259,10 @@ def main():
     ap.add_argument("study")
     ap.add_argument("--frame", type=int, default=0)
     ap.add_argument("--loops", type=int, default=16)
+    ap.add_argument("--das-precision", type=int, default=0, choices=[0, 1],
+                    help="1: HERCULES DAS from the FP16 interpolation table")
     a = ap.parse_args()
-    print(json.dumps(throughput(a.base, a.study, frame=a.frame, loops=a.loops)))
+    print(json.dumps(throughput(a.base, a.study, frame=a.frame, loops=a.loops, das_precision=a.das_precision)))
 
 
 if __name__ == "__main__":

@@ -205,3 +205,21 @@ def test_filter_precision_argument_checks(lib):
     assert lib.beamformer_gb300_set_das_precision(-1) == 0
     for p in (1, 0):
         assert lib.beamformer_gb300_set_das_precision(p) == 1
+    from ogl_beamforming_cuda_gb300.client import Beamformer, BeamformerError
+    with pytest.raises(BeamformerError):
+        Beamformer().set_precision(das=2)
+    with pytest.raises(BeamformerError):
+        Beamformer().set_precision(filter=5)
+    assert Beamformer().set_precision(filter=0, das=0) is not None
+
+
+def test_server_rejects_bad_arguments():
+    """ogl_beamformer_server refuses an unknown option and a DAS precision out of
+    range before it creates the shared-memory region (no GPU needed)."""
+    exe = os.path.join(ROOT, "ogl_beamforming_cuda_gb300", "lib", "ogl_beamformer_server")
+    if not os.path.exists(exe):
+        pytest.skip("server not built")
+    r = subprocess.run([exe, "--bogus"], capture_output=True, text=True, timeout=30)
+    assert r.returncode == 2 and "usage" in r.stderr
+    r = subprocess.run([exe, "--das-precision", "7"], capture_output=True, text=True, timeout=30)
+    assert r.returncode == 2 and "unsupported" in r.stderr.lower()
