@@ -38,6 +38,14 @@
  *
  * Sample indices stay bit-equal to the reference's: the delay chain is the same
  * sequence of round-to-nearest operations as das_kernel's.
+ *
+ * DAS precision 1 (DasParams::half_table, the precision variant; H in the
+ * templates) trades that exactness for speed within about -57 dB of the FP32
+ * volume: the table in FP16 pairs scaled by a power of two from the frame's
+ * largest channel-data magnitude (chan_absmax), segments evaluated in packed
+ * FP16, the sample index sqrt(x) fs / c + io from an approximate reciprocal
+ * square root, a degree-3 apodization, and a thread's two depths in packed FP32
+ * pairs; sums stay FP32.
  */
 #include "bf_kernels.h"
 #include "bf_das_math.cuh"

@@ -68,6 +68,38 @@ __device__ __forceinline__ __half2 as_half2(unsigned u)
 	return h;
 }
 
+/* Precision 1: sample value of one term from the FP16 table at index ic (cubic
+ * and linear: ic in [0, s_lim); nearest: round(ic) inside the row), and the
+ * fraction the phase rotation needs. */
+template <int INTERP>
+__device__ __forceinline__ void sample_half(const float4 *__restrict__ tab, int row, float ic, float &f, float &vx,
+                                            float &vy)
+{
+	float2 v;
+	if (INTERP == INTERP_NEAREST) {
+		const float r = roundf(ic);
+		v = __half22float2(__ldg((const __half2 *)tab + (row + (int)r)));
+		f = ic - r;
+	} else {
+		const int ii = (int)ic;
+		f = ic - (float)ii;
+		const __half2 f2 = __float2half2_rn(f);
+		__half2 h;
+		if (INTERP == INTERP_CUBIC) {
+			const uint4 q = __ldg((const uint4 *)tab + (unsigned)(row + ii));
+			h = __hfma2(as_half2(q.w), f2, as_half2(q.z));
+			h = __hfma2(h, f2, as_half2(q.y));
+			h = __hfma2(h, f2, as_half2(q.x));
+		} else {
+			const uint2 q = __ldg((const uint2 *)tab + (unsigned)(row + ii));
+			h = __hfma2(as_half2(q.y), f2, as_half2(q.x));
+		}
+		v = __half22float2(h);
+	}
+	vx = v.x;
+	vy = v.y;
+}
+
 /* The part of one (voxel, transmit t, receive r) term after the lateral distance:
  * lat2 = |lateral offset|^2 of the virtual element (r, t); row = (r * T + t) * S.
  * ROT: the table is rotated (DasParams::rot_table), the term by theta (f - 1/2)
@@ -106,35 +138,18 @@ __device__ __forceinline__ void term_tail(const DasParams &p, const float4 *__re
 	const float a  = ok ? (H ? apod_cos2_p3(w) : apod_cos2_p5(w)) * scale : 0.0f;
 	const float ic = ok ? idx : 1.0f;
 	float vx, vy, f = 0.0f;
-	if (H) {
-		/* FP16 table: index clamped to the table (nearest outside the proof may
-		 * round to the sample after the last row's end, which reads 0) */
-		if (INTERP == INTERP_NEAREST) {
-			const float r = roundf(ic);
-			const int j = row + (int)r;
-			const int last = p.C * p.T * p.S - 1;
-			const float2 v = __half22float2(__ldg((const __half2 *)tab + min(j, last)));
-			vx = INR || j <= last ? v.x : 0.0f;
-			vy = INR || j <= last ? v.y : 0.0f;
-			f = ic - r;
-		} else {
-			const int ii = (int)ic;
-			f = ic - (float)ii;
-			const __half2 f2 = __float2half2_rn(f);
-			__half2 h;
-			if (INTERP == INTERP_CUBIC) {
-				const uint4 q = __ldg((const uint4 *)tab + (unsigned)(row + ii));
-				h = __hfma2(as_half2(q.w), f2, as_half2(q.z));
-				h = __hfma2(h, f2, as_half2(q.y));
-				h = __hfma2(h, f2, as_half2(q.x));
-			} else {
-				const uint2 q = __ldg((const uint2 *)tab + (unsigned)(row + ii));
-				h = __hfma2(as_half2(q.y), f2, as_half2(q.x));
-			}
-			const float2 v = __half22float2(h);
-			vx = v.x;
-			vy = v.y;
-		}
+	if (H && INTERP == INTERP_NEAREST && !INR) {
+		/* FP16 table, nearest outside the proof: round(idx) may be the sample
+		 * after the last row's end, which reads 0 */
+		const float r = roundf(ic);
+		const int j = row + (int)r;
+		const int last = p.C * p.T * p.S - 1;
+		const float2 v = __half22float2(__ldg((const __half2 *)tab + min(j, last)));
+		vx = j <= last ? v.x : 0.0f;
+		vy = j <= last ? v.y : 0.0f;
+		f = ic - r;
+	} else if (H) {
+		sample_half<INTERP>(tab, row, ic, f, vx, vy);
 	} else if (INTERP == INTERP_NEAREST && INR) {
 		/* round(idx) proven inside the row: no bound check; with ROT the sample
 		 * comes pre-rotated by its phase from the table (float2 per sample) */
@@ -306,41 +321,11 @@ __device__ __forceinline__ void hercules_column(const DasParams &p, const float4
 	}
 }
 
-/* Precision 1: sample value of one term from the FP16 table at index ic (proven
- * in range), and the fraction the phase rotation needs. */
-template <int INTERP>
-__device__ __forceinline__ void sample_half(const float4 *__restrict__ tab, int row, float ic, float &f, float &vx,
-                                            float &vy)
-{
-	float2 v;
-	if (INTERP == INTERP_NEAREST) {
-		const float r = roundf(ic);
-		v = __half22float2(__ldg((const __half2 *)tab + (row + (int)r)));
-		f = ic - r;
-	} else {
-		const int ii = (int)ic;
-		f = ic - (float)ii;
-		const __half2 f2 = __float2half2_rn(f);
-		__half2 h;
-		if (INTERP == INTERP_CUBIC) {
-			const uint4 q = __ldg((const uint4 *)tab + (unsigned)(row + ii));
-			h = __hfma2(as_half2(q.w), f2, as_half2(q.z));
-			h = __hfma2(h, f2, as_half2(q.y));
-			h = __hfma2(h, f2, as_half2(q.x));
-		} else {
-			const uint2 q = __ldg((const uint2 *)tab + (unsigned)(row + ii));
-			h = __hfma2(as_half2(q.y), f2, as_half2(q.x));
-		}
-		v = __half22float2(h);
-	}
-	vx = v.x;
-	vy = v.y;
-}
-
 /* Precision 1, one transmit of two depths of a column (the float2 lanes are the
  * two voxels) whose sample indices are proven in range: the per-voxel arithmetic
  * of term_tail<..., INR, H> in packed FP32 (per component the same IEEE
- * operations as the scalar forms). ROT != 0 or !DEMOD. */
+ * operations as its scalar form; the caller forms the lateral distance with
+ * FMAs). ROT != 0 or !DEMOD. */
 template <int INTERP, bool DEMOD, int ROT>
 __device__ __forceinline__ void term_h2(const DasParams &p, const float4 *__restrict__ tab, float lat2, float2 dz2,
                                         float2 ka2, float2 io, int row, float scale, float2 &ax, float2 &ay)
