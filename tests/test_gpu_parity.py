@@ -200,7 +200,6 @@ def test_beamform_data_synchronized_matches_oracle():
     bp = small_params(S=512, C=32, T=32, points=(32, 1, 32))
     raw = small_raw(bp)
     from ogl_beamforming_cuda_gb300.client import Beamformer
-    from oracle.bf_oracle import OraclePipeline
     bf = Beamformer().configure(bp, [SH["Decode"], SH["Demodulate"], SH["DAS"]], kaiser=(5.65, 5e6, 25e6, 32))
     vol = bf.beamform(raw)
     orc = oracle_for(bf, bp, [SH["Decode"], SH["Demodulate"], SH["DAS"]], kaiser=(5.65, 5e6, 25e6, 32))
