@@ -108,3 +108,28 @@ def test_batch_with_half_table(interp):
         orc.interpolation = interp
         db = nrmse(out[i].cpu().numpy(), orc.compute(raw)["frame"])
         assert db <= BOUND_DB, (i, db)
+
+
+def test_mixed_pipeline_through_the_reference_abi():
+    """The whole mixed pipeline (FP16 decode output + tensor-core FIR, FP16 DAS
+    table) through beamform_data_synchronized with a 4-frame Sum, against the
+    oracle's FP32 pipeline on the same frames."""
+    bp = small_params(S=1024, C=32, T=32, points=(16, 4, 32), D=2, frames=4)
+    pipe = [SH["Decode"], SH["Demodulate"], SH["DAS"], SH["Sum"]]
+    raws = [small_raw(bp, seed=60 + k, n_points=12, n_speckle=300) for k in range(4)]
+    bf = Beamformer().configure(bp, pipe, kaiser=KAISER, interpolation=1)
+    bf.set_precision(filter=1, das=1)
+    try:
+        for raw in raws[:-1]:
+            bf.push(raw)
+        vol = bf.beamform(raws[-1])
+    finally:
+        bf.set_precision(filter=0, das=0)
+    orc = oracle_for(bf, bp, pipe, kaiser=KAISER)
+    orc.interpolation = 1
+    ref = None
+    for raw in raws:
+        ref = orc.compute(raw)["averaged"]
+    db = nrmse(vol, ref)
+    print(f"mixed pipeline, 4-frame sum: {db:.1f} dB")
+    assert db <= BOUND_DB, db
