@@ -43,6 +43,15 @@ DAS_BYTES_PER_TERM = 32            # cubic sample-op: four complex f32 samples r
 L1_BYTES_PER_CLK_SM = 128          # L1/shared-memory data path per SM per clock
 
 
+def _ok(ret, what):
+    """A library call's boolean result: raise with the library's error string on 0
+    (plain asserts would vanish under python -O, and with them the calls)."""
+    if not ret:
+        from ogl_beamforming_cuda_gb300 import abi
+        raise RuntimeError(f"{what} failed: {abi.load().beamformer_get_last_error_string().decode()}")
+    return ret
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -82,8 +91,8 @@ def profile_frames(args):
     points = tuple(int(v) for v in args.points.split(","))
     bp, pipe, kaiser = workload(points)
     bf = Beamformer().configure(bp, pipe, kaiser=kaiser)
-    assert bf.lib.beamformer_gb300_set_filter_precision(args.precision)
-    assert bf.lib.beamformer_gb300_set_das_precision(args.precision)
+    _ok(bf.lib.beamformer_gb300_set_filter_precision(args.precision), "set_filter_precision")
+    _ok(bf.lib.beamformer_gb300_set_das_precision(args.precision), "set_das_precision")
     raw = torch.from_numpy(synth.acquisition(bp, 1000, n_points=N_POINTS, n_speckle=args.speckle, device="cuda:0"))
     raw = raw.to("cuda:0")
     for _ in range(args.profile_frames):
@@ -282,9 +291,10 @@ def run_ours(args, rank, world, local, dist):
 
     def e2e_step():
         for f in range(FRAMES - 1):
-            assert L.beamformer_push_data_with_compute(ctypes.c_void_p(host[f].data_ptr()), nbytes, 0)
-        assert L.beamform_data_synchronized(ctypes.c_void_p(host[FRAMES - 1].data_ptr()), nbytes, pts,
-                                            ctypes.cast(out.data_ptr(), ctypes.POINTER(ctypes.c_float)), -1)
+            _ok(L.beamformer_push_data_with_compute(ctypes.c_void_p(host[f].data_ptr()), nbytes, 0), "push_data_with_compute")
+        _ok(L.beamform_data_synchronized(ctypes.c_void_p(host[FRAMES - 1].data_ptr()), nbytes, pts,
+                                         ctypes.cast(out.data_ptr(), ctypes.POINTER(ctypes.c_float)), -1),
+            "beamform_data_synchronized")
 
     e2e_step()
     torch.cuda.synchronize()
@@ -306,7 +316,8 @@ def run_ours(args, rank, world, local, dist):
     mixed = None
     if rank == 0:
         ref_vol = out.numpy().astype(np.float64)
-        assert L.beamformer_gb300_set_filter_precision(1) and L.beamformer_gb300_set_das_precision(1)
+        _ok(L.beamformer_gb300_set_filter_precision(1), "set_filter_precision")
+        _ok(L.beamformer_gb300_set_das_precision(1), "set_das_precision")
         dev = host.to(f"cuda:{local}")
 
         def mstep():
@@ -326,7 +337,8 @@ def run_ours(args, rank, world, local, dist):
         torch.cuda.synchronize()
         m_te = (time.perf_counter() - h0) / max(args.steps, 1)
         m_vol = out.numpy().astype(np.float64)
-        assert L.beamformer_gb300_set_filter_precision(0) and L.beamformer_gb300_set_das_precision(0)
+        _ok(L.beamformer_gb300_set_filter_precision(0), "set_filter_precision")
+        _ok(L.beamformer_gb300_set_das_precision(0), "set_das_precision")
         db = float(20 * np.log10(np.sqrt(np.mean((m_vol - ref_vol) ** 2) / np.mean(ref_vol ** 2))))
         mixed = {"value": 1e3 / m_ms, "unit": "volumes/s", "e2e": 1.0 / m_te if args.steps else None,
                  "das_ms": (m_stages.get("DASFast") or 0.0) * 1e3,
@@ -425,8 +437,8 @@ def run_precision(args, peaks):
     res = {}
     for prec, name in ((0, "fp32"), (1, "fp16"), (2, "bf16")):
         bf = Beamformer().configure(bp, pipe, kaiser=kaiser, interpolation=2)
-        assert bf.lib.beamformer_gb300_set_filter_precision(prec)
-        assert bf.lib.beamformer_gb300_set_das_precision(1 if prec else 0)
+        _ok(bf.lib.beamformer_gb300_set_filter_precision(prec), "set_filter_precision")
+        _ok(bf.lib.beamformer_gb300_set_das_precision(1 if prec else 0), "set_das_precision")
         stream = torch.cuda.ExternalStream(bf.lib.beamformer_gb300_get_stream())
         push = lambda: bf.push_device(raw.data_ptr(), raw.numel() * 2)
         for _ in range(max(args.warmup, 3)):
@@ -492,8 +504,8 @@ def _precision_volume(args):
     out, vols = {}, {}
     for name, fp, dp in (("fp32", 0, 0), ("mixed", 1, 1)):
         bf = Beamformer().configure(bp, pipe, kaiser=kaiser)
-        assert bf.lib.beamformer_gb300_set_filter_precision(fp)
-        assert bf.lib.beamformer_gb300_set_das_precision(dp)
+        _ok(bf.lib.beamformer_gb300_set_filter_precision(fp), "set_filter_precision")
+        _ok(bf.lib.beamformer_gb300_set_das_precision(dp), "set_das_precision")
         stream = torch.cuda.ExternalStream(bf.lib.beamformer_gb300_get_stream())
 
         def step():
@@ -667,7 +679,7 @@ def run_learned(args, peaks):
     # the fallback's arithmetic: full-aperture DAS from the FP16 table (DAS
     # precision 1) where its volume is within -40 dB of the FP32 one, else FP32
     full32 = pm.das(raw, 1).clone()
-    assert pm.bf.lib.beamformer_gb300_set_das_precision(1)
+    _ok(pm.bf.lib.beamformer_gb300_set_das_precision(1), "set_das_precision")
     try:
         db_mixed = Lm.nrmse_db(pm.das(raw, 1), full32)
         torch.cuda.synchronize()
