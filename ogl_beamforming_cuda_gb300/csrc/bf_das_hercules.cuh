@@ -48,9 +48,11 @@ __device__ __forceinline__ float apod_cos2_p3(float w)
 }
 
 /* Table scale of DAS precision 1: the shift k with m 2^k in [1024, 2048) for the
- * largest channel-data magnitude m (float bits); 0 when m is 0, below 2^-100,
- * above 2^100 or not a number. Every FP16 coefficient and Horner partial sum is
- * then below 17 m 2^k < 2^15 (the cubic coefficients sum to at most 17 m). */
+ * largest channel-data component m (float bits); 0 when m is 0, below 2^-100,
+ * above 2^100 or not a number. Each component of a cubic segment's coefficients
+ * is at most 1, 1, 9 and 6 m before the rotation, so every rotated coefficient
+ * and Horner partial sum is below 17 sqrt(2) m 2^k < 49300, inside FP16's
+ * largest finite 65504. */
 __device__ __forceinline__ int half_table_shift(unsigned m_bits)
 {
 	const float m = __uint_as_float(m_bits);
