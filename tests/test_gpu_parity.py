@@ -175,17 +175,21 @@ def test_sum_and_min_max_bit_exact():
     from oracle.bf_oracle import OraclePipeline
     bf = Beamformer().configure(bp, pipe, kaiser=(5.65, 5e6, 25e6, 32))
     orc = oracle_for(bf, bp, pipe, kaiser=(5.65, 5e6, 25e6, 32))
+    gpu_frames = []
     for seed in range(6):       # more frames than averaged: the ring wraps
         raw = small_raw(bp, seed=seed)
         bf.push(raw)
         ref = orc.compute(raw)
-    bf.synchronize()
+        bf.synchronize()
+        gpu_frames.append(bf.frame(0)[0].copy())
     das, _ = bf.frame(0)
     check_volume(das, ref["frame"], "DAS frame")
     avg, _ = bf.frame(1)
     check_volume(avg, ref["averaged"], "averaged frame")
     # sum and min/max themselves are bit exact: feed the GPU frames to the oracle
     from oracle import bf_oracle as O
+    expect = O.sum_frames(gpu_frames[-4:], np.float32(1.0) / np.float32(4), (64, 2, 64))
+    assert np.array_equal(avg.view(np.uint32), expect.view(np.uint32)), "Sum not bit-exact"
     levels = O.min_max(das, (64, 2, 64))
     off = 0
     mips = O.frame_mips((64, 2, 64))
@@ -245,3 +249,38 @@ def test_min_max_pyramid_shapes(dims):
         got, d = bf.frame(0, lvl)
         assert np.array_equal(got, levels[off:off + got.size], equal_nan=True), f"mip {lvl} of {dims}"
         off += got.size
+
+
+def transformed_xdc(bp, z_degrees, scale, x_degrees=0.0):
+    """xdc_transform with a rotation about z (then about x), scaled, translation
+    kept: the transducer frame the reference applies per voxel (das.glsl:182,
+    220, 263). The stored matrix is column-major: X[column][row]."""
+    X = np.asarray(bp.xdc_transform[:], np.float64).reshape(4, 4)
+    a, b = np.radians(z_degrees), np.radians(x_degrees)
+    rz = np.array([[np.cos(a), -np.sin(a), 0], [np.sin(a), np.cos(a), 0], [0, 0, 1]])
+    rx = np.array([[1, 0, 0], [0, np.cos(b), -np.sin(b)], [0, np.sin(b), np.cos(b)]])
+    M = scale * (rx @ rz)                       # row-major M[row][column]
+    X[:3, :3] = M.T
+    bp.xdc_transform[:] = X.astype(np.float32).ravel().tolist()
+    return bp
+
+
+XDC_CASES = [(25.0, 1.1, 0.0), (-40.0, 0.8, 0.0), (15.0, 1.0, 8.0)]
+
+
+@pytest.mark.parametrize("z_deg,scale,x_deg", XDC_CASES)
+@pytest.mark.parametrize("interp", (0, 1, 2))
+@pytest.mark.parametrize("kernel", ("hercules", "generic", "forces"))
+def test_das_rotated_scaled_transducer_transform(monkeypatch, z_deg, scale, x_deg, interp, kernel):
+    """A rotated and scaled (and, in the last case, tilted) xdc_transform through
+    the HERCULES fast path (its per-voxel range proof works in transducer
+    coordinates), the general kernel and FORCES, against the oracle."""
+    if kernel == "generic":
+        monkeypatch.setenv("OGL_BF_DAS_GENERIC", "1")
+    das = "FORCES" if kernel == "forces" else "HERCULES"
+    bp = transformed_xdc(small_params(S=1024, C=16, T=16, points=(20, 4, 24), das=das), z_deg, scale, x_deg)
+    raw = small_raw(bp, n_points=10, n_speckle=200)
+    shader = SH["DASFast"] if kernel == "hercules" else SH["DAS"]
+    bf, ref = run_both(bp, [SH["Decode"], SH["Demodulate"], shader], raw, interpolation=interp)
+    assert np.any(ref["frame"] != 0)
+    check_volume(bf.frame(0)[0], ref["frame"], f"{kernel} xdc rot z {z_deg} x {x_deg} scale {scale} interp={interp}")
