@@ -417,12 +417,23 @@ LIB_FN uint32_t beamformer_gb300_batch_tuning(int32_t *volume_tiles, int32_t *ct
  *   channel_data    device, float2 [channel][transmit][sample];
  *   frame           device, output_points[0..2] float2 in x-fastest order;
  *   cuda_stream     cudaStream_t as a pointer (NULL: the default stream).
- * The partial sums of small volumes are kept in a static device array of
- * 262144 float2 entries (2 MiB) that every GPU loading this library holds
- * until the process exits. A call that would need more (channel groups times
- * voxels > 262144) fails with BF_LIB_ERR_KIND_BUFFER_OVERFLOW. The first call on
- * a device looks up the array's device address; make that first call before any
- * stream capture. All calls share the array, so calls that overlap on the GPU race. */
+ * The two host tables are read before the call returns; they travel to the GPU
+ * as kernel parameters, so the caller may reuse them at once.
+ * The call is self-contained: das_parameters->interpolate selects nearest (0)
+ * or cubic (non-zero) interpolation, every receive channel is summed, and the
+ * library-wide settings of set_interpolation, set_receive_subsampling and
+ * set_das_precision do not apply to it.
+ * Small volumes split the receive channels into groups whose partial sums are
+ * kept in a static device array of 262144 float2 entries (2 MiB) that every GPU
+ * loading this library holds until the process exits. The call uses as many
+ * groups as that array holds for the volume, down to one group, which writes
+ * the frame directly and needs no partial sums, so no volume is refused for
+ * lack of room. The first call on a device looks up the array's device
+ * address; make that first call before any stream capture. After a
+ * cudaDeviceReset, call beamformer_gb300_shutdown() before the next call so
+ * that the address is looked up again. All calls share the array and the
+ * tables, which keep the last call's contents, so calls that overlap on the
+ * GPU race. */
 LIB_FN uint32_t beamformer_gb300_das_no_alloc(const BeamformerParameters *das_parameters, const float *focal_vectors,
                                               const int16_t *sparse_elements, const void *channel_data,
                                               uint64_t channel_data_bytes, float *frame, void *cuda_stream);

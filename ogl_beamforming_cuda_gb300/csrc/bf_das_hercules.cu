@@ -237,7 +237,8 @@ cudaError_t launch_das_table(const DasParams &p, float4 *table, cudaStream_t s)
 	if (das_hercules_table_bytes(p) == 0) return cudaSuccess;
 	if (!table || (p.half_table && !p.absmax)) return cudaErrorInvalidValue;
 	const int64_t entries = (int64_t)p.C * p.T * p.S;
-	const int blocks = (int)((entries + 255) / 256 < 152 * 16 ? (entries + 255) / 256 : 152 * 16);
+	const int64_t most = (int64_t)device_sm_count() * 16;
+	const int blocks = (int)((entries + 255) / 256 < most ? (entries + 255) / 256 : most);
 	if (p.half_table) {
 		/* the scale: every sample the table reads, rf[0, min(readable, entries + 2)) */
 		const int64_t n = p.rf_count < entries + 2 ? p.rf_count : entries + 2;

@@ -396,7 +396,7 @@ cudaError_t launch_fir_tc(const void *x, uint32_t rows, uint32_t row_samples, ui
 	p.error = error;
 	const int row_blocks = (int)((rows + TC_M - 1) / TC_M);
 	/* at least ~4 CTAs per SM's worth of work, at least 4 output blocks per CTA */
-	int splits = (4 * 152 + row_blocks - 1) / row_blocks;
+	int splits = (4 * device_sm_count() + row_blocks - 1) / row_blocks;
 	splits = std::min(splits, std::max(1, p.q_blocks / 4));
 	p.splits = splits;
 	const size_t smem = 1024 + (size_t)TC_RING * TC_ATOM_BYTES + (size_t)p.atoms * N * 128 + (TC_RING + 3) * 8;

@@ -299,14 +299,14 @@ cudaError_t launch_analytic(const float2 *in, float2 *out, int64_t rows, uint32_
 		if (e != cudaSuccess) return e;
 		if (per_sm < 1) return cudaErrorInvalidConfiguration;
 		const int64_t ctas_needed = (rows + rpc - 1) / rpc;
-		const int64_t max_blocks = 152LL * per_sm;
+		const int64_t max_blocks = (int64_t)device_sm_count() * per_sm;
 		const int blocks = (int)(ctas_needed < max_blocks ? ctas_needed : max_blocks);
 		analytic_rows_stockham<<<blocks, 256, smem, s>>>(in, out, rows, (int)samples, rpc, twiddles);
 	} else {
 		const size_t smem = (size_t)samples * sizeof(float2);
 		const cudaError_t e = cudaFuncSetAttribute(analytic_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 		if (e != cudaSuccess) return e;
-		const int64_t max_blocks = 152;
+		const int64_t max_blocks = device_sm_count();
 		const int blocks = (int)(rows < max_blocks ? rows : max_blocks);
 		analytic_rows<<<blocks, 256, smem, s>>>(in, out, rows, log2n, twiddles);
 	}

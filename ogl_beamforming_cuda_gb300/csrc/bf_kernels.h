@@ -180,6 +180,7 @@ cudaError_t launch_das_table(const DasParams &p, float4 *table, cudaStream_t s);
  * capacity in float2 partial-sum entries (groups x voxels) */
 cudaError_t launch_das_no_alloc(DasParams p, const float4 *focal4, const int16_t *sparse, cudaStream_t s);
 int64_t     das_no_alloc_capacity();
+void        das_no_alloc_forget_devices();
 
 /* CudaHilbert stage (bf_hilbert.cu): analytic signal of each of `rows` rows of
  * `samples` complex values (real parts used), in -> out; samples a power of two
@@ -192,5 +193,9 @@ cudaError_t launch_analytic(const float2 *in, float2 *out, int64_t rows, uint32_
 
 /* kernel launches issued since load (all launchers count here) */
 extern uint64_t g_kernel_launches;
+
+/* Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount,
+ * looked up once per device); 1 if the query fails. Grid sizes follow it. */
+int device_sm_count();
 
 } /* namespace bf */

@@ -741,10 +741,7 @@ bool fill_das_params(const Plan &pl, int kind, const void *rf, uint64_t rf_bytes
  * (2-7 % faster than 19). */
 int32_t hercules_per_group(const DasParams &p)
 {
-	int dev = 0, sms = 0;
-	if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-	    sms <= 0)
-		sms = 152;
+	const int sms = device_sm_count();
 	const double slots = (double)sms * das_hercules_blocks_per_sm(p);
 	const int64_t tiles = das_hercules_tiles(p);
 	const double terms = (double)p.T * p.loop_end / (p.rx_step > 0 ? p.rx_step : 1);
@@ -1305,9 +1302,7 @@ bool build_batch(const BeamformerParameters *params, uint32_t count, const void 
 
 	/* autotuner: every (tile shape, CTAs per SM) candidate runs the batch once to
 	 * warm up and once timed; the fastest is kept */
-	int sms = 152;
-	int dev = 0;
-	if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	const int sms = device_sm_count();
 	const bool tile_choices[2] = {true, false};
 	const int cta_choices[3] = {4, 5, 6};
 	gb.ctas_general = 8 * sms;
@@ -1683,7 +1678,10 @@ LIB_FN uint32_t beamformer_gb300_set_interpolation(int32_t mode)
 /* See include/ogl_beamformer_lib.h. Allocates nothing: no cudaMalloc, no
  * cudaFree, no allocating library call; the partial sums and the focal/sparse
  * tables live in static device arrays of bf_das.cu. Divisions and square roots
- * take the IEEE path, which the allocated path's faster forms equal bit for bit. */
+ * take the IEEE path, which the allocated path's faster forms equal bit for bit.
+ * The call is self-contained: das_parameters->interpolate selects nearest or
+ * cubic, every receive channel is summed, and the library-wide settings of
+ * set_interpolation, set_receive_subsampling and set_das_precision do not apply. */
 LIB_FN uint32_t beamformer_gb300_das_no_alloc(const BeamformerParameters *das_parameters, const float *focal_vectors,
                                               const int16_t *sparse_elements, const void *channel_data,
                                               uint64_t channel_data_bytes, float *frame, void *cuda_stream)
@@ -1751,7 +1749,19 @@ LIB_FN uint32_t beamformer_gb300_das_no_alloc(const BeamformerParameters *das_pa
 		p.per_group = (int32_t)((p.loop_end + want - 1) / want);
 		p.groups = (p.loop_end + p.per_group - 1) / p.per_group;
 	}
+	/* as many channel groups as the static partial-sum array holds (at least one:
+	 * a single group writes the frame directly and needs no partial sums) */
 	const int64_t nv = (int64_t)p.dims[0] * p.dims[1] * p.dims[2];
+	if (p.groups > 1 && (int64_t)p.groups * nv > das_no_alloc_capacity()) {
+		const int64_t fit = das_no_alloc_capacity() / nv;
+		if (fit <= 1) {
+			p.groups = 1;
+			p.per_group = p.loop_end;
+		} else {
+			p.per_group = (int32_t)((p.loop_end + fit - 1) / fit);
+			p.groups = (p.loop_end + p.per_group - 1) / p.per_group;
+		}
+	}
 	if (p.groups > 1 && (int64_t)p.groups * nv > das_no_alloc_capacity()) return fail(BF_LIB_ERR_KIND_BUFFER_OVERFLOW);
 	float4 focal[256];
 	for (int i = 0; i < 256; i++) {
@@ -1768,6 +1778,7 @@ LIB_FN uint64_t beamformer_gb300_kernel_launch_count(void) { return g_kernel_lau
 
 LIB_FN void beamformer_gb300_shutdown(void)
 {
+	das_no_alloc_forget_devices();
 	if (!g.ready) return;
 	cudaDeviceSynchronize();
 	free_batch();

@@ -106,7 +106,8 @@ min_max_fused(const float2 *__restrict__ src, float2 *__restrict__ levels, const
 static int grid_for(int64_t n)
 {
 	int64_t g = (n + 255) / 256;
-	return (int)(g < 152 * 16 ? (g < 1 ? 1 : g) : 152 * 16);
+	const int64_t most = (int64_t)device_sm_count() * 16;
+	return (int)(g < most ? (g < 1 ? 1 : g) : most);
 }
 
 static int orone(int x) { return x ? x : 1; }

@@ -369,7 +369,7 @@ synth_k(const float *__restrict__ pos, const float *__restrict__ amp, int n_scat
 	for (int i = threadIdx.x; i < S; i += blockDim.x) dst[i] = trace[i];
 }
 
-int grid_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 152 * 32); }
+int grid_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, (int64_t)device_sm_count() * 32); }
 
 } /* namespace */
 } /* namespace bf */

@@ -484,7 +484,7 @@ void bfo_decode(const BfoDecodeUBO *u, int32_t variant, int32_t first_stage, int
 	float   *outf       = (float *)out;
 	uint32_t xs = dispatch[0] * 4, cs = dispatch[1];
 	uint32_t ts = dispatch[2] * 16;
-	if (ts > T) ts = T; /* transmits beyond the order are not decoded (see DESIGN) */
+	if (ts > T) ts = T; /* transmits beyond the Hadamard order are not decoded */
 
 	/* pass 1: gather the raw data into [channel][sample index][transmit] */
 	uint64_t scratch_elems = 0;

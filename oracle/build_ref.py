@@ -20,9 +20,12 @@ is git-ignored.
   zemp_probe        the zemp_bp_v1 typedef of tests/throughput.c (the captured-
                     dataset parameter block), cut out by name and compiled into
                     a program printing its size and field offsets.
+  parameters_layout.txt  field offsets of BeamformerParameters and the sizes of
+                    its sibling structs, printed by a probe that includes the
+                    reference's beamformer_parameters.h.
 
-Usage: python oracle/build_ref.py [--reference PATH]. Exits 0 and builds nothing
-when the reference checkout is absent.
+Usage: python oracle/build_ref.py --reference PATH (or BF_REFERENCE_DIR=PATH).
+Exits 0 and builds nothing when no checkout is given or it is absent.
 """
 import argparse
 import os
@@ -48,6 +51,11 @@ FILTER_VARIANTS = [
     ("demod_f32", ["INPUT_DATA_TYPE_FLOAT", "DEMODULATE"]),
 ]
 DAS_VARIANTS = [("das_full", ["DAS_FAST 0"]), ("das_fast", ["DAS_FAST 1"])]
+PARAMETER_FIELDS = ("xdc_transform", "dec_data_dim", "xdc_element_pitch", "rf_raw_dim", "transmit_mode", "decode",
+                    "das_shader_id", "time_offset", "output_min_coordinate", "output_max_coordinate", "output_points",
+                    "sampling_frequency", "center_frequency", "speed_of_sound", "off_axis_pos", "beamform_plane",
+                    "f_number", "interpolate", "coherency_weighting", "decimation_rate", "readi_group_id",
+                    "readi_group_size")
 
 DECODE_UBO = """
 static uint input_channel_stride, input_sample_stride, input_transmit_stride;
@@ -190,12 +198,32 @@ def build(ref):
         run(["gcc", "-std=c11", probe, "-o", os.path.join(OUT, "zemp_probe")])
     run(cc + [os.path.join(ref, "helpers", "ogl_beamformer_lib.c"), "-o", os.path.join(OUT, "libref_client.so"),
               "-lm"])
+    # layout of the reference's BeamformerParameters family (beamformer_parameters.h):
+    # a probe that includes the header where it lies prints field offsets and sizes
+    probe = os.path.join(OUT, "parameters_probe.c")
+    with open(probe, "w") as f:
+        f.write("#include <stdio.h>\n#include <stddef.h>\n#include <stdint.h>\n"
+                f'#include "{os.path.join(ref, "beamformer_parameters.h")}"\n'
+                "#define O(f) printf(#f \" %zu\\n\", offsetof(BeamformerParameters, f));\n"
+                "int main(void) {\n" + "".join(f"\tO({n})\n" for n in PARAMETER_FIELDS) +
+                "\tprintf(\"size %zu %zu %zu %zu %zu\\n\", sizeof(BeamformerParameters), "
+                "sizeof(BeamformerUIParameters), sizeof(BeamformerParametersHead), "
+                "sizeof(BeamformerComputeStatsTable), sizeof(BeamformerLiveImagingParameters));\n"
+                "\treturn 0;\n}\n")
+    run(["gcc", "-std=c11", probe, "-o", os.path.join(OUT, "parameters_probe")])
+    layout = subprocess.run([os.path.join(OUT, "parameters_probe")], check=True, capture_output=True, text=True).stdout
+    with open(os.path.join(OUT, "parameters_layout.txt"), "w") as f:
+        f.write(layout)
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("BF_REFERENCE_DIR", "/root/reference"))
+    ap.add_argument("--reference", default=os.environ.get("BF_REFERENCE_DIR"),
+                    help="path of the reference checkout (default: $BF_REFERENCE_DIR)")
     args = ap.parse_args()
+    if not args.reference:
+        print("no reference checkout given (--reference or BF_REFERENCE_DIR); oracle/_ref not built")
+        return 0
     if not os.path.isdir(os.path.join(args.reference, "shaders")):
         print(f"reference checkout not found at {args.reference}; oracle/_ref not built")
         return 0

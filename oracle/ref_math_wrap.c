@@ -31,8 +31,9 @@ static Arena ref_arena(void)
 }
 
 /* Copies `count` ints starting at the returned matrix. On x86 the reference's
- * Kronecker product writes outside the dim*dim block (see DESIGN), so callers
- * may ask for more than dim*dim entries to see everything it wrote. */
+ * Kronecker product (orders 12 2^k and 20 2^k) writes outside the dim*dim block
+ * through its unparenthesised store macro, so callers may ask for more than
+ * dim*dim entries to see everything it wrote. */
 int ref_hadamard(int dim, int *out, int count)
 {
 	Arena a = ref_arena();
