@@ -34,6 +34,7 @@ sys.path.insert(0, ROOT)
 
 FRAMES = 16
 POINTS = (128, 128, 256)
+PLANE = (128, 1, 128)
 S, C, T = 2048, 128, 128
 FILTER_TAPS = 64
 N_POINTS, N_SPECKLE = 200, 20000
@@ -204,31 +205,31 @@ def algorithmic_bytes():
     }
 
 
-def fp32_peak_tflops(peaks):
-    """Nominal FP32 FMA throughput: 152 SMs x 128 lanes x 2 flops x max SM clock.
+def fp32_peak_tflops(peaks, sms):
+    """Nominal FP32 FMA throughput: SMs x 128 lanes x 2 flops x max SM clock.
     MEASURED_PEAKS.json carries no FP32 figure, so the measured max clock is used."""
     mhz = float(peaks.get("sm_max_mhz", 2070.0))
-    return 152 * 128 * 2 * mhz * 1e6 / 1e12
+    return sms * 128 * 2 * mhz * 1e6 / 1e12
 
 
-def l1_peak_gbs(peaks):
-    """Nominal L1/shared-memory bandwidth: 152 SMs x 128 B x max SM clock."""
-    mhz = float(peaks.get("sm_max_mhz", 2070.0))
-    return 152 * L1_BYTES_PER_CLK_SM * mhz * 1e6 / 1e9
-
-
-def das_roofline(das_t, peaks, traffic):
+def das_roofline(das_t, peaks, traffic, shared_gbs, sms):
     """DAS is bound by min(FP32 peak / 40 flops, L1 bandwidth / 32 B) per cubic
     sample-op (one (voxel, transmit, receive) term); for cubic the L1 term is the
-    smaller, so the roofline is stated in L1 bytes."""
+    smaller, so the roofline is stated in L1 bytes. The L1 peak is measured on
+    the device (beamformer_gb300_measure_shared_bandwidth: conflict-free LDS.128
+    streaming on every SM, CUDA events); without it, the nominal 128 B per clock
+    per SM at the measured max clock."""
     ops = int(np.prod(POINTS)) * T * C
-    fp32 = fp32_peak_tflops(peaks)
-    l1 = l1_peak_gbs(peaks)
+    fp32 = fp32_peak_tflops(peaks, sms)
+    nominal = sms * L1_BYTES_PER_CLK_SM * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e9
+    l1 = shared_gbs or nominal
+    src = ("measured: shared-memory streaming kernel (LDS.128, conflict-free, all SMs, CUDA events); "
+           f"nominal {sms} x 128 B/clk x sm_max_mhz = {nominal:.0f} GB/s" if shared_gbs else
+           f"nominal {sms} x 128 B/clk x sm_max_mhz of MEASURED_PEAKS.json")
     ops_fp32, ops_l1 = fp32 * 1e12 / DAS_FLOPS_PER_TERM, l1 * 1e9 / DAS_BYTES_PER_TERM
     out = {"kernel": "das_hercules<cubic> (+ its interpolation-table pass)", "sample_ops_per_launch": ops,
            "bytes_per_sample_op": DAS_BYTES_PER_TERM, "flops_per_sample_op": DAS_FLOPS_PER_TERM,
-           "peak_source": "nominal from sm_max_mhz of MEASURED_PEAKS.json (it holds no L1 or FP32 figure): "
-                          "L1 152 x 128 B/clk, FP32 152 x 128 x 2 flop/clk",
+           "peak_source": src, "fp32_peak_source": f"nominal {sms} x 128 x 2 flop/clk x sm_max_mhz",
            "traffic": traffic, "das_ms": das_t * 1e3 if das_t else None}
     if ops_l1 <= ops_fp32:
         out.update(bound="l1", unit="GB/s", peak=l1,
@@ -240,6 +241,54 @@ def das_roofline(das_t, peaks, traffic):
     out["fp32_tflops"] = ops * DAS_FLOPS_PER_TERM / das_t / 1e12 if das_t else None
     out["fp32_frac"] = out["fp32_tflops"] / fp32 if das_t else None
     return out
+
+
+def run_plane(args, local):
+    """The plane workload on the GPU through the C ABI: planes/s with four distinct
+    seeded acquisitions resident in HBM (268 MB, larger than L2) pushed in turn,
+    and end to end with beamform_data_synchronized from pinned host memory."""
+    import torch
+    from ogl_beamforming_cuda_gb300 import synth
+    from ogl_beamforming_cuda_gb300.client import Beamformer
+    bp, pipe, kaiser = plane_workload()
+    bf = Beamformer().configure(bp, pipe, kaiser=kaiser, interpolation=2)
+    dev = f"cuda:{local}"
+    frames = torch.stack([torch.from_numpy(synth.acquisition(bp, 2000 + k, n_points=20)) for k in range(4)]).to(dev)
+    nbytes = frames[0].numel() * 2
+    stream = torch.cuda.ExternalStream(bf.lib.beamformer_gb300_get_stream())
+    steps = max(args.steps, 1) * 8
+
+    def step():
+        for k in range(4):
+            bf.push_device(frames[k].data_ptr(), nbytes)
+    for _ in range(max(args.warmup, 3)):
+        step()
+    bf.synchronize()
+    ms = _events_ms(step, stream, steps) / 4
+    stages = {k: v * 1e3 for k, v in stage_times(bf, 4 * steps).items()}
+    host = frames.cpu().pin_memory()
+    del frames
+    vox = int(np.prod(PLANE))
+    out = torch.empty(2 * vox, dtype=torch.float32).pin_memory()
+    pts = (ctypes.c_int32 * 3)(*PLANE)
+    L = bf.lib
+
+    def e2e():
+        for k in range(4):
+            _ok(L.beamform_data_synchronized(ctypes.c_void_p(host[k].data_ptr()), nbytes, pts,
+                                             ctypes.cast(out.data_ptr(), ctypes.POINTER(ctypes.c_float)), -1),
+                "beamform_data_synchronized")
+    e2e()
+    torch.cuda.synchronize()
+    h0 = time.perf_counter()
+    for _ in range(steps):
+        e2e()
+    te = (time.perf_counter() - h0) / (4 * steps)
+    return {"workload": "HERCULES RCA 128+128, 128 tx, 2048 samples int16 -> decode -> demod(64 taps, decimation 2) "
+                        "-> linear DAS 128x1x128 x-z plane", "value": 1e3 / ms, "unit": "planes/s",
+            "ms_per_plane": ms, "e2e": {"value": 1.0 / te, "unit": "planes/s", "h2d_bytes_per_step": nbytes,
+                                        "d2h_bytes_per_step": 8 * vox},
+            "stage_ms": stages, "l2": "four distinct 67 MB acquisitions resident (268 MB > L2), pushed in turn"}
 
 
 def run_ours(args, rank, world, local, dist):
@@ -344,18 +393,28 @@ def run_ours(args, rank, world, local, dist):
                  "das_ms": (m_stages.get("DASFast") or 0.0) * 1e3,
                  "nrmse_db_vs_fp32_volume": db, "bound_db": -40.0,
                  "arithmetic": "FP16 decode output + tcgen05 FIR, FP16 DAS interpolation table, FP32 sums"}
+    plane = run_plane(args, local) if rank == 0 else None
+    bw = ctypes.c_double(0.0)
+    shared_gbs = bw.value / 1e9 if L.beamformer_gb300_measure_shared_bandwidth(ctypes.byref(bw)) else None
     return dict(t=t, te=te, stages=stages, launches=launches, clocks=clk.summary(), nbytes=nbytes, out_bytes=8 * vox,
-                mixed=mixed)
+                mixed=mixed, plane=plane, shared_gbs=shared_gbs, sms=torch.cuda.get_device_properties(local).multi_processor_count)
 
 
-def cpu_sample(budget_s=12.0):
-    """Volumes/s of the CPU oracle (reference semantics, all host cores), estimated
-    from a bounded sample: decode and demodulation of 4 of the 128 channels, DAS
-    of voxel ranges spread over the volume, and the full sum and min/max; each
-    part scaled to a full 16-frame volume."""
+CPU_STRATA, CPU_RUNS_PER_STRATUM, CPU_RUN = 16, 4, 256
+
+
+def cpu_sample():
+    """Volumes/s of the CPU oracle (reference semantics, all host cores) on a
+    fixed sample of the 3D workload, scaled to a whole 16-frame volume: decode
+    and demodulation of 4 of the 128 channels, DAS of 64 fixed runs of 256 voxels
+    (16 depth strata x 4 lateral positions: shallow and deep, central and edge
+    voxels, whose active apertures differ), and the full Sum and MinMax. The same
+    voxels every time, so repeated samples time the same work. Returns the
+    extrapolated rate and the sample's own wall time."""
     from oracle import bf_oracle as O
     from ogl_beamforming_cuda_gb300 import synth
     threads = O.threads()
+    t_start = time.perf_counter()
     bp, pipe, kaiser = workload()
     csub = 4
     sub = synth.make_parameters(samples=S, channels=csub, transmits=T, points=POINTS, decimation=2, interpolate=1,
@@ -376,36 +435,61 @@ def cpu_sample(budget_s=12.0):
     sparse = np.arange(256, dtype=np.int16)
     V = int(np.prod(POINTS))
     frame = np.zeros(2 * V, np.float32)
-    # stratified random runs of voxels: one run per stratum of V / ranges voxels,
-    # so shallow and deep, central and edge voxels (whose active aperture differs)
-    # are all represented
-    ranges = 16
-    srng = np.random.default_rng(1)
-    stratum = V // ranges
-
-    def das_runs(per):
-        t0 = time.perf_counter()
-        for i in range(ranges):
-            v0 = stratum * i + int(srng.integers(0, max(1, stratum - per)))
-            O.das(plan.das, rf, POINTS, sparse, focal, fast=True, voxel_begin=v0, voxel_end=v0 + per, out=frame)
-        return time.perf_counter() - t0
-
-    per = 256           # long enough runs for the oracle's threads to share evenly
-    probe = das_runs(per)
-    per = int(max(256, min(stratum, per * (0.6 * budget_s) / max(probe, 1e-3))))
-    t_das = das_runs(per) * V / (ranges * per)
+    X, Y, Z = POINTS
+    slices = Z // CPU_STRATA
+    t0 = time.perf_counter()
+    for i in range(CPU_STRATA):
+        z = i * slices + slices // 2
+        for j in range(CPU_RUNS_PER_STRATUM):
+            y = (2 * j + 1) * Y // (2 * CPU_RUNS_PER_STRATUM) - 1
+            v0 = (z * Y + y) * X
+            O.das(plan.das, rf, POINTS, sparse, focal, fast=True, voxel_begin=v0, voxel_end=v0 + CPU_RUN, out=frame)
+    voxels = CPU_STRATA * CPU_RUNS_PER_STRATUM * CPU_RUN
+    t_das = (time.perf_counter() - t0) * V / voxels
 
     frames = [np.zeros(2 * V, np.float32) for _ in range(FRAMES)]
     t0 = time.perf_counter()
     O.sum_frames(frames, np.float32(1 / FRAMES), POINTS)
     O.min_max(frames[0], POINTS)
     t_tail = time.perf_counter() - t0
-    t_volume = FRAMES * (t_front + t_das + t_tail)
-    sample = (f"decode+demod of {csub}/{C} channels, DAS of {ranges * per}/{V} voxels in {ranges} stratified "
-              f"random runs, "
-              f"full sum+min_max; scaled to {FRAMES} frames (extrapolated)")
+    t_volume = FRAMES * (t_front + t_das) + t_tail
+    sample = (f"decode+demod of {csub}/{C} channels, DAS of {voxels}/{V} voxels in {CPU_STRATA} depth strata x "
+              f"{CPU_RUNS_PER_STRATUM} fixed runs, full sum+min_max; scaled to one {FRAMES}-frame volume "
+              f"(extrapolated x {V / voxels:.0f} in DAS voxels)")
     return {"value": 1.0 / t_volume, "unit": "volumes/s", "cores": threads, "kind": "port", "sample": sample,
-            "seconds_per_volume": t_volume}
+            "seconds_per_volume": t_volume, "sample_wall_s": time.perf_counter() - t_start}
+
+
+def plane_workload():
+    """The plane configuration: the same acquisition (128 tx, 128 rx, 2048
+    samples, 64-tap Kaiser, decimation 2) beamformed to a 128 x 1 x 128 x-z plane
+    with linear interpolation, one frame per step."""
+    from ogl_beamforming_cuda_gb300 import synth
+    bp = synth.make_parameters(samples=S, channels=C, transmits=T, points=PLANE, decimation=2, f_number=1.0,
+                               interpolate=0, filter_length=FILTER_TAPS)
+    return bp, synth.default_pipeline(), synth.kaiser_spec(FILTER_TAPS)
+
+
+def cpu_plane(reps=1):
+    """Planes/s of the CPU oracle running the whole plane workload (decode,
+    demodulation, linear DAS of every voxel) on all host cores: no extrapolation."""
+    from oracle import bf_oracle as O
+    from ogl_beamforming_cuda_gb300 import synth
+    bp, pipe, kaiser = plane_workload()
+    raw = synth.acquisition(bp, 2000, n_points=20)
+    orc = O.OraclePipeline()
+    orc.bp, orc.shaders = bp, list(pipe)
+    orc.create_kaiser(*kaiser, 0)
+    orc.interpolation = 2
+    walls = []
+    for _ in range(max(reps, 1)):
+        t0 = time.perf_counter()
+        orc.compute(raw)
+        walls.append(time.perf_counter() - t0)
+    t = statistics.median(walls)
+    return {"value": 1.0 / t, "unit": "planes/s", "cores": O.threads(), "kind": "port",
+            "sample": "the whole plane: decode, demodulation and linear DAS of all 16384 voxels (not extrapolated)",
+            "seconds_per_plane": t, "runs": len(walls)}
 
 
 def _events_ms(fn, stream, reps):
@@ -731,22 +815,29 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
-        samples = []
         for _ in range(max(args.warmup, 0)):
-            cpu_sample(budget_s=2.0)
-        for _ in range(max(args.steps, 1)):
-            samples.append(cpu_sample(budget_s=3.0))
+            cpu_sample()
+        samples = [cpu_sample() for _ in range(max(args.steps, 1))]
         v = statistics.median(s["value"] for s in samples)
+        wall = statistics.median(s["sample_wall_s"] for s in samples)
         cb = dict(samples[0])
         cb["value"] = v
-        print(json.dumps({
+        line = {
             "impl": "reference", "metric": METRIC, "value": v, "unit": "volumes/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config_dict({"reference_arm": "CPU restatement of the reference shaders (oracle); the "
-                                   "reference's GLSL path needs an OpenGL context, unavailable on this box"}),
+            "config": config_dict(),
+            "reference_arm": "CPU restatement of the reference shaders (oracle, pinned bit-exact to the shader "
+                             "source); the reference's GLSL path needs an OpenGL context, unavailable on this box",
+            "step": "one fixed sample of the 3D volume (ms_per_step is its wall time); value is that sample "
+                    "scaled to a whole 16-frame volume",
+            "extrapolated_seconds_per_volume": 1.0 / v,
+            "sample_values": [s["value"] for s in samples],
             "cpu_baseline": cb,
-            "e2e": {"value": v, "unit": "volumes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+            "e2e": {"value": v, "unit": "volumes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        if not args.no_cpu_baseline:
+            line["plane_workload"] = cpu_plane()
+        print(json.dumps(line))
         return 0
 
     dist = None
@@ -781,7 +872,7 @@ def main():
         "e2e": {"value": e2e, "unit": "volumes/s", "h2d_bytes_per_step": FRAMES * r["nbytes"],
                 "d2h_bytes_per_step": r["out_bytes"]},
         "gpu_launches": r["launches"],
-        "roofline": das_roofline(das_t, peaks, traffic),
+        "roofline": das_roofline(das_t, peaks, traffic, r.get("shared_gbs"), r["sms"]),
         "stages": stage_roof,
         "clocks": r["clocks"],
     }
@@ -789,8 +880,12 @@ def main():
         m = dict(r["mixed"])
         m["speedup_vs_fp32"] = m["value"] / (value / world)     # rank 0 alone runs the mixed pipeline
         line["mixed_precision"] = m
+    if r.get("plane"):
+        line["plane_workload"] = r["plane"]
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample()
+        if r.get("plane"):
+            line["plane_workload"]["cpu_baseline"] = cpu_plane()
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

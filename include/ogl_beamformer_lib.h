@@ -438,6 +438,13 @@ LIB_FN uint32_t beamformer_gb300_das_no_alloc(const BeamformerParameters *das_pa
                                               const int16_t *sparse_elements, const void *channel_data,
                                               uint64_t channel_data_bytes, float *frame, void *cuda_stream);
 
+/* Measured bandwidth of the GPU's shared-memory (L1) data path in bytes per
+ * second, the roofline denominator of delay-and-sum: a conflict-free 16-byte-per-
+ * lane streaming kernel on every SM, timed with CUDA events (best of six after
+ * two warm-ups, about 0.1 s). A measurement aid with no counterpart in the
+ * reference; it changes no clock or power setting. */
+LIB_FN uint32_t beamformer_gb300_measure_shared_bandwidth(double *bytes_per_second);
+
 /* Number of kernel launches this library issued since load (all streams). */
 LIB_FN uint64_t beamformer_gb300_kernel_launch_count(void);
 

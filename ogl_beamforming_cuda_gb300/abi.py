@@ -108,6 +108,7 @@ SIGNATURES = [
     ("beamformer_gb300_batch_tuning", u32, [P(i32), P(i32), P(f32), i32, P(i32)]),
     ("beamformer_gb300_das_no_alloc", u32, [P(BeamformerParameters), P(f32), P(ctypes.c_int16), vp, ctypes.c_uint64,
                                        vp, vp]),
+    ("beamformer_gb300_measure_shared_bandwidth", u32, [P(ctypes.c_double)]),
     ("beamformer_gb300_kernel_launch_count", ctypes.c_uint64, []),
     ("beamformer_gb300_shutdown", None, []),
 ]

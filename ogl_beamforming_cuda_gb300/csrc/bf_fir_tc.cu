@@ -35,6 +35,7 @@
 #include <cudaTypedefs.h>
 #include <cuda_fp16.h>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -57,6 +58,8 @@ struct FirTcParams {
 	int32_t       x_first;      /* -E: real-sample coordinate of block 0's window */
 	uint32_t      idesc;        /* tcgen05 instruction descriptor */
 	unsigned     *error;        /* set to 1 when a wait runs out */
+	long long     stall_cycles; /* > 0 (tests only): the first wait is on a barrier nothing
+	                               arrives at, bounded by this many cycles, so it runs out */
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -72,7 +75,7 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
 }
 
 /* bounded wait for the phase with the given parity to complete */
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long limit = TC_WAIT_CYCLES)
 {
 	const long long t0 = clock64();
 	while (true) {
@@ -82,7 +85,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
 		             "selp.u32 %0, 1, 0, p;\n\t}"
 		             : "=r"(done) : "r"(bar), "r"(parity) : "memory");
 		if (done) return true;
-		if (clock64() - t0 > TC_WAIT_CYCLES) return false;
+		if (clock64() - t0 > limit) return false;
 	}
 }
 
@@ -175,6 +178,7 @@ fir_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtenso
 	const int total_atoms = nq + p.atoms - 1;
 
 	const uint32_t full0 = smem_u32(bars), mma0 = smem_u32(bars + TC_RING), gbar = smem_u32(bars + TC_RING + 2);
+	const uint32_t never = smem_u32(bars + TC_RING + 3);        /* no thread or copy arrives here */
 	/* two accumulator buffers of N f32 columns; allocations are powers of two >= 32 */
 	constexpr uint32_t tcols = N <= 16 ? 32u : N <= 32 ? 64u : 128u;
 	if (warp == 0) {
@@ -187,6 +191,7 @@ fir_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtenso
 		mbar_init(mma0, 1);
 		mbar_init(mma0 + 8, 1);
 		mbar_init(gbar, 1);
+		mbar_init(never, 1);
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 		stop = 0;
 	}
@@ -223,7 +228,7 @@ fir_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtenso
 		mbar_expect_tx(gbar, (uint32_t)(p.atoms * N * 128));
 		for (int a = 0; a < p.atoms; a++) tma_load_2d(smem_u32(gsm) + (uint32_t)(a * N * 128), &gmap, 64 * a, 0, gbar);
 		for (; issued < total_atoms && issued < TC_RING; issued++) issue_atom(issued);
-		ok = mbar_wait(gbar, 0) && mma_block(0);
+		ok = (p.stall_cycles <= 0 || mbar_wait(never, 0, p.stall_cycles)) && mbar_wait(gbar, 0) && mma_block(0);
 		if (!ok) stop = 1;
 	}
 	__syncthreads();
@@ -268,7 +273,9 @@ fir_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtenso
 	__syncthreads();
 	if (tid == 0 && stop) {
 		atomicExch(p.error, 1u);
-		/* drain the loads still in flight before the shared memory is released */
+		/* drain the loads still in flight (the tap table and the ring's atoms)
+		 * before the shared memory is released */
+		mbar_wait(gbar, 0);
 		for (int a = max(0, issued - TC_RING); a < issued; a++)
 			mbar_wait(full0 + 8 * (a % TC_RING), (uint32_t)((a / TC_RING) & 1));
 	}
@@ -394,12 +401,15 @@ cudaError_t launch_fir_tc(const void *x, uint32_t rows, uint32_t row_samples, ui
 	const uint32_t ab = bf16 ? 1u : 0u;
 	p.idesc = (1u << 4) | (ab << 7) | (ab << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
 	p.error = error;
+	/* test hook: OGL_BF_TEST_FIR_STALL_CYCLES=n makes every CTA's first wait run out
+	 * after n cycles (the error word is then set and the kernel stops early) */
+	if (const char *stall = std::getenv("OGL_BF_TEST_FIR_STALL_CYCLES")) p.stall_cycles = std::atoll(stall);
 	const int row_blocks = (int)((rows + TC_M - 1) / TC_M);
 	/* at least ~4 CTAs per SM's worth of work, at least 4 output blocks per CTA */
 	int splits = (4 * device_sm_count() + row_blocks - 1) / row_blocks;
 	splits = std::min(splits, std::max(1, p.q_blocks / 4));
 	p.splits = splits;
-	const size_t smem = 1024 + (size_t)TC_RING * TC_ATOM_BYTES + (size_t)p.atoms * N * 128 + (TC_RING + 3) * 8;
+	const size_t smem = 1024 + (size_t)TC_RING * TC_ATOM_BYTES + (size_t)p.atoms * N * 128 + (TC_RING + 4) * 8;
 	static bool attr = false;
 	if (!attr) {
 		cudaFuncSetAttribute(fir_tc<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);

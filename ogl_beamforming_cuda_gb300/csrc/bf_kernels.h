@@ -198,4 +198,8 @@ extern uint64_t g_kernel_launches;
  * looked up once per device); 1 if the query fails. Grid sizes follow it. */
 int device_sm_count();
 
+/* Measured bandwidth of the shared-memory data path (conflict-free LDS.128 from
+ * every SM, best of six event-timed launches after two warm-ups). */
+cudaError_t measure_shared_bandwidth(double *bytes_per_second, cudaStream_t s);
+
 } /* namespace bf */

@@ -1774,6 +1774,13 @@ LIB_FN uint32_t beamformer_gb300_das_no_alloc(const BeamformerParameters *das_pa
 	return cuda_ok(launch_das_no_alloc(p, focal, sparse, (cudaStream_t)cuda_stream)) ? 1 : 0;
 }
 
+LIB_FN uint32_t beamformer_gb300_measure_shared_bandwidth(double *bytes_per_second)
+{
+	if (!bytes_per_second) return fail(BF_LIB_ERR_KIND_INVALID_ACCESS);
+	if (!ensure_cuda()) return 0;
+	return cuda_ok(measure_shared_bandwidth(bytes_per_second, g.stream)) ? 1 : 0;
+}
+
 LIB_FN uint64_t beamformer_gb300_kernel_launch_count(void) { return g_kernel_launches; }
 
 LIB_FN void beamformer_gb300_shutdown(void)

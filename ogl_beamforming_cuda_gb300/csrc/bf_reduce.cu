@@ -165,3 +165,61 @@ cudaError_t launch_min_max(const float2 *level0, const int32_t dims[3], int mips
 }
 
 } /* namespace bf */
+
+namespace bf {
+
+/* Shared-memory streaming probe (the measured peak of the L1/shared-memory data
+ * path that bounds delay-and-sum): every warp reads 32 consecutive 16-byte words
+ * per LDS.128 (conflict-free, 128 bytes per quarter-warp wavefront), eight loads
+ * in flight per thread, two logic operations per load to keep them alive. */
+__global__ void __launch_bounds__(256) shared_stream(int iters, unsigned *sink)
+{
+	__shared__ uint4 buf[2048];                                  /* 32 KB */
+	for (int i = threadIdx.x; i < 2048; i += blockDim.x)
+		buf[i] = make_uint4(i, 3u * i + 1u, 5u * i + 2u, 7u * i + 3u);
+	__syncthreads();
+	unsigned a = 0, b = 0;
+	int k = threadIdx.x;
+	for (int it = 0; it < iters; it++) {
+		const uint4 *q = buf + (k & 1023);
+		#pragma unroll
+		for (int u = 0; u < 8; u++) {
+			const uint4 v = q[u * 128];
+			a ^= v.x ^ v.y;
+			b ^= v.z ^ v.w;
+		}
+		k += 32;
+	}
+	if ((a ^ b) == 0x9E3779B9u) atomicAdd(sink, 1u);
+}
+
+cudaError_t measure_shared_bandwidth(double *bytes_per_second, cudaStream_t s)
+{
+	constexpr int ITERS = 20000, THREADS = 256;
+	const int blocks = device_sm_count() * 4;
+	unsigned *sink = nullptr;
+	cudaEvent_t e0 = nullptr, e1 = nullptr;
+	cudaError_t e = cudaMalloc(&sink, sizeof(unsigned));
+	if (e == cudaSuccess) e = cudaEventCreate(&e0);
+	if (e == cudaSuccess) e = cudaEventCreate(&e1);
+	float best = 0.0f;
+	for (int rep = 0; rep < 8 && e == cudaSuccess; rep++) {
+		cudaEventRecord(e0, s);
+		shared_stream<<<blocks, THREADS, 0, s>>>(ITERS, sink);
+		g_kernel_launches++;
+		cudaEventRecord(e1, s);
+		if ((e = cudaEventSynchronize(e1)) != cudaSuccess) break;
+		float ms = 0.0f;
+		if ((e = cudaEventElapsedTime(&ms, e0, e1)) != cudaSuccess) break;
+		if (rep >= 2 && (best == 0.0f || ms < best)) best = ms;     /* two warm-up runs */
+	}
+	if (e == cudaSuccess) e = cudaGetLastError();
+	if (e == cudaSuccess)
+		*bytes_per_second = (double)blocks * THREADS * ITERS * 8 * 16 / (best * 1e-3);
+	if (e0) cudaEventDestroy(e0);
+	if (e1) cudaEventDestroy(e1);
+	if (sink) cudaFree(sink);
+	return e;
+}
+
+} /* namespace bf */

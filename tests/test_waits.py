@@ -59,3 +59,33 @@ def test_rf_ring_full_with_zero_timeout():
     L.beamformer_set_global_timeout(-1)
     assert L.beamformer_push_data_with_compute(raw.ctypes.data, raw.nbytes, 0) == 1
     assert bf.synchronize()
+
+
+def test_tensor_core_fir_wait_that_runs_out_is_reported(monkeypatch):
+    """The tcgen05 FIR's mbarrier waits are bounded. A test hook makes each CTA's
+    first wait one on a barrier that nothing arrives at, limited to ~1 ms: the
+    wait runs out, the CTA drains the loads it issued and stops, and
+    beamformer_gb300_synchronize reports the error word (CUDA_RUNTIME). The next
+    compute without the hook runs normally and matches the oracle."""
+    from bf_cases import small_params, small_raw, oracle_for
+    bp = small_params(S=1024, C=32, T=32, points=(16, 1, 24), D=2)
+    raw = small_raw(bp)
+    kaiser = (5.65, 5e6, 25e6, 32)
+    pipe = [SH["Decode"], SH["Demodulate"], SH["DAS"]]
+    bf = Beamformer().configure(bp, pipe, kaiser=kaiser)
+    L = bf.lib
+    assert L.beamformer_gb300_set_filter_precision(1)
+    try:
+        monkeypatch.setenv("OGL_BF_TEST_FIR_STALL_CYCLES", "2000000")
+        assert L.beamformer_push_data_with_compute(raw.ctypes.data, raw.nbytes, 0) == 1
+        assert L.beamformer_gb300_synchronize(-1) == 0
+        assert L.beamformer_get_last_error() == abi.ERR["CUDA_RUNTIME"]
+        monkeypatch.delenv("OGL_BF_TEST_FIR_STALL_CYCLES")
+        bf.push(raw)
+        assert L.beamformer_gb300_synchronize(-1) == 1
+        vol = bf.frame(0)[0].copy()
+    finally:
+        L.beamformer_gb300_set_filter_precision(0)
+    ref = oracle_for(bf, bp, pipe, kaiser=kaiser).compute(raw)["frame"]
+    from conftest import nrmse_db
+    assert nrmse_db(vol, ref) <= -60.0
