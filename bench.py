@@ -65,6 +65,9 @@ def parse():
                     help="only push this many copies of one device-resident frame through the pipeline "
                          "(for a profiler), print per-stage ms and exit")
     ap.add_argument("--points", default=",".join(map(str, POINTS)), help="voxel grid for --profile-frames")
+    ap.add_argument("--keep-voxel-size", action="store_true",
+                    help="for --profile-frames: shrink the output extent with the grid so voxels keep the "
+                         "workload's size (a smaller case of the same kernel for a profiler)")
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1],
                     help="for --profile-frames: 1 runs the mixed pipeline (FP16 front end, FP16 DAS table)")
     ap.add_argument("--variant", default="plain", choices=["plain", "precision", "batched", "learned"],
@@ -76,10 +79,18 @@ def parse():
     return ap.parse_args()
 
 
-def workload(points=POINTS):
+WORKLOAD_EXTENT = ((-5e-3, -5e-3, 5e-3), (5e-3, 5e-3, 25e-3))
+
+
+def workload(points=POINTS, keep_voxel_size=False):
     from ogl_beamforming_cuda_gb300 import synth
-    bp = synth.make_parameters(samples=S, channels=C, transmits=T, points=points, decimation=2, f_number=1.0,
-                               interpolate=1, frames=FRAMES, filter_length=FILTER_TAPS)
+    extent = WORKLOAD_EXTENT
+    if keep_voxel_size:
+        lo, hi = np.asarray(WORKLOAD_EXTENT[0]), np.asarray(WORKLOAD_EXTENT[1])
+        mid, half = (lo + hi) / 2, (hi - lo) / 2 * np.asarray(points) / np.asarray(POINTS)
+        extent = (tuple(mid - half), tuple(mid + half))
+    bp = synth.make_parameters(samples=S, channels=C, transmits=T, points=points, extent=extent, decimation=2,
+                               f_number=1.0, interpolate=1, frames=FRAMES, filter_length=FILTER_TAPS)
     return bp, synth.default_pipeline(sum_and_minmax=True), synth.kaiser_spec(FILTER_TAPS)
 
 
@@ -90,7 +101,7 @@ def profile_frames(args):
     from ogl_beamforming_cuda_gb300.client import Beamformer
     torch.cuda.set_device(0)
     points = tuple(int(v) for v in args.points.split(","))
-    bp, pipe, kaiser = workload(points)
+    bp, pipe, kaiser = workload(points, args.keep_voxel_size)
     bf = Beamformer().configure(bp, pipe, kaiser=kaiser)
     _ok(bf.lib.beamformer_gb300_set_filter_precision(args.precision), "set_filter_precision")
     _ok(bf.lib.beamformer_gb300_set_das_precision(args.precision), "set_das_precision")
@@ -400,17 +411,18 @@ def run_ours(args, rank, world, local, dist):
                 mixed=mixed, plane=plane, shared_gbs=shared_gbs, sms=torch.cuda.get_device_properties(local).multi_processor_count)
 
 
-CPU_STRATA, CPU_RUNS_PER_STRATUM, CPU_RUN = 16, 4, 256
+CPU_STRATA, CPU_RUN = 16, 4096
 
 
 def cpu_sample():
     """Volumes/s of the CPU oracle (reference semantics, all host cores) on a
     fixed sample of the 3D workload, scaled to a whole 16-frame volume: decode
-    and demodulation of 4 of the 128 channels, DAS of 64 fixed runs of 256 voxels
-    (16 depth strata x 4 lateral positions: shallow and deep, central and edge
-    voxels, whose active apertures differ), and the full Sum and MinMax. The same
-    voxels every time, so repeated samples time the same work. Returns the
-    extrapolated rate and the sample's own wall time."""
+    and demodulation of 4 of the 128 channels, DAS of 16 fixed runs of 4096
+    voxels (one per depth stratum, alternately at the edge and in the centre of
+    the lateral grid, whose active apertures differ; runs this long keep the
+    oracle's per-call threading overhead below a few per cent), and the full Sum
+    and MinMax. The same voxels every time, so repeated samples time the same
+    work. Returns the extrapolated rate and the sample's own wall time."""
     from oracle import bf_oracle as O
     from ogl_beamforming_cuda_gb300 import synth
     threads = O.threads()
@@ -438,13 +450,13 @@ def cpu_sample():
     X, Y, Z = POINTS
     slices = Z // CPU_STRATA
     t0 = time.perf_counter()
+    rows = CPU_RUN // X
     for i in range(CPU_STRATA):
         z = i * slices + slices // 2
-        for j in range(CPU_RUNS_PER_STRATUM):
-            y = (2 * j + 1) * Y // (2 * CPU_RUNS_PER_STRATUM) - 1
-            v0 = (z * Y + y) * X
-            O.das(plan.das, rf, POINTS, sparse, focal, fast=True, voxel_begin=v0, voxel_end=v0 + CPU_RUN, out=frame)
-    voxels = CPU_STRATA * CPU_RUNS_PER_STRATUM * CPU_RUN
+        y = 0 if i % 2 == 0 else (Y - rows) // 2
+        v0 = (z * Y + y) * X
+        O.das(plan.das, rf, POINTS, sparse, focal, fast=True, voxel_begin=v0, voxel_end=v0 + CPU_RUN, out=frame)
+    voxels = CPU_STRATA * CPU_RUN
     t_das = (time.perf_counter() - t0) * V / voxels
 
     frames = [np.zeros(2 * V, np.float32) for _ in range(FRAMES)]
@@ -453,9 +465,9 @@ def cpu_sample():
     O.min_max(frames[0], POINTS)
     t_tail = time.perf_counter() - t0
     t_volume = FRAMES * (t_front + t_das) + t_tail
-    sample = (f"decode+demod of {csub}/{C} channels, DAS of {voxels}/{V} voxels in {CPU_STRATA} depth strata x "
-              f"{CPU_RUNS_PER_STRATUM} fixed runs, full sum+min_max; scaled to one {FRAMES}-frame volume "
-              f"(extrapolated x {V / voxels:.0f} in DAS voxels)")
+    sample = (f"decode+demod of {csub}/{C} channels, DAS of {voxels}/{V} voxels in {CPU_STRATA} fixed runs (one per "
+              f"depth stratum, edge and central rows alternately), full sum+min_max; scaled to one {FRAMES}-frame "
+              f"volume (extrapolated x {V / voxels:.0f} in DAS voxels)")
     return {"value": 1.0 / t_volume, "unit": "volumes/s", "cores": threads, "kind": "port", "sample": sample,
             "seconds_per_volume": t_volume, "sample_wall_s": time.perf_counter() - t_start}
 

@@ -50,6 +50,10 @@
 #include "bf_kernels.h"
 #include "bf_das_math.cuh"
 #include "bf_das_hercules.cuh"
+#include "bf_das_staged.cuh"
+
+#include <cstdlib>
+#include <cstring>
 
 namespace bf {
 
@@ -154,6 +158,48 @@ das_hercules(DasParams p, const float4 *__restrict__ tab)
 	hercules_tile<INTERP, TY, herc_threads<TY>(), H>(p, tab, blockIdx.x, yt, blockIdx.z, blockIdx.y - yt * p.groups);
 }
 
+/* The staged form (bf_das_staged.cuh): cubic and linear tables, 8 blocks of 128
+ * threads per SM with about 27 KB of shared memory each. */
+template <int INTERP, int TY, bool H>
+__global__ void __launch_bounds__(128, 8)
+das_hercules_staged(DasParams p, const float4 *__restrict__ tab)
+{
+	extern __shared__ __align__(128) uint8_t stg_smem[];
+	const int yt = blockIdx.y / p.groups;
+	hercules_tile_staged<INTERP, TY, H>(p, tab, blockIdx.x, yt, blockIdx.z, blockIdx.y - yt * p.groups, stg_smem);
+}
+
+/* volume tile of the staged kernel: HercTile<4> (4 x 4 x 16) unless
+ * OGL_BF_DAS_STAGED_TILE=8 (4 x 8 x 8, for comparisons) */
+static int staged_volume_ty()
+{
+	const char *env = std::getenv("OGL_BF_DAS_STAGED_TILE");
+	return env && env[0] == '8' ? 8 : 4;
+}
+
+/* the staged kernel runs for FP32 cubic and linear tables (the FP16 table of DAS
+ * precision 1 measured faster unstaged: 52.5 against 60.8 ms per 3D frame);
+ * OGL_BF_DAS_STAGED=0 keeps hercules_tile (for comparisons), =1 stages the FP16
+ * table of volumes too, =require marks blocks that cannot stage with NaN (tests) */
+static bool use_staged(const DasParams &p)
+{
+	const char *env = std::getenv("OGL_BF_DAS_STAGED");
+	if (env && env[0] == '0') return false;
+	if (p.interp != INTERP_CUBIC && p.interp != INTERP_LINEAR) return false;
+	if (p.half_table && !(env && (env[0] == '1' || env[0] == 'r'))) return false;
+	if (p.half_table && p.dims[1] < 4) return false;
+	return p.wait_error != nullptr && p.T <= 256 && p.loop_end <= 256 && (p.rot_table != 0 || !(p.fc > 0.0f));
+}
+
+template <int INTERP, int TY, bool H>
+static int staged_occupancy()
+{
+	int n = 0;
+	const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, das_hercules_staged<INTERP, TY, H>, 128,
+	                                                                    stg_smem_bytes<INTERP, TY, H>());
+	return e == cudaSuccess && n > 0 ? n : 1;
+}
+
 int64_t das_hercules_table_bytes(const DasParams &p)
 {
 	const int64_t n = (int64_t)p.C * p.T * p.S;
@@ -165,6 +211,11 @@ int64_t das_hercules_table_bytes(const DasParams &p)
 
 int64_t das_hercules_tiles(const DasParams &p)
 {
+	if (p.dims[1] >= 4 && use_staged(p) && staged_volume_ty() == 8) {
+		using T = HercTile<8, 128>;
+		return (int64_t)((p.dims[0] + T::X - 1) / T::X) * ((p.dims[1] + T::Y - 1) / T::Y) *
+		       ((p.dims[2] + T::Z * T::NV - 1) / (T::Z * T::NV));
+	}
 	if (p.dims[1] >= 4) {
 		using T = HercTile<4, herc_threads<4>()>;
 		return (int64_t)((p.dims[0] + T::X - 1) / T::X) * ((p.dims[1] + T::Y - 1) / T::Y) *
@@ -189,8 +240,22 @@ static int hercules_occupancy(int interp)
 
 int das_hercules_blocks_per_sm(const DasParams &p)
 {
-	static int cache[2][3][2] = {};
+	static int cache[2][3][2] = {}, staged[2][2][2] = {};
 	const int ty = p.dims[1] >= 4 ? 1 : 0, ip = p.interp >= 0 && p.interp < 3 ? p.interp : 0, h = p.half_table ? 1 : 0;
+	if (use_staged(p)) {
+		/* every staged form fits 8 blocks of 128 threads per SM at 64 registers and
+		 * about 27 KB of shared memory; the query confirms it per form */
+		int &s = staged[ty][p.interp == INTERP_CUBIC ? 1 : 0][h];
+		if (!s) {
+			if (p.interp == INTERP_CUBIC)
+				s = ty ? (h ? staged_occupancy<INTERP_CUBIC, 4, true>() : staged_occupancy<INTERP_CUBIC, 4, false>())
+				       : (h ? staged_occupancy<INTERP_CUBIC, 1, true>() : staged_occupancy<INTERP_CUBIC, 1, false>());
+			else
+				s = ty ? (h ? staged_occupancy<INTERP_LINEAR, 4, true>() : staged_occupancy<INTERP_LINEAR, 4, false>())
+				       : (h ? staged_occupancy<INTERP_LINEAR, 1, true>() : staged_occupancy<INTERP_LINEAR, 1, false>());
+		}
+		return s;
+	}
 	int &c = cache[ty][ip][h];
 	if (!c) c = ty ? (h ? hercules_occupancy<4, true>(p.interp) : hercules_occupancy<4, false>(p.interp))
 	               : (h ? hercules_occupancy<1, true>(p.interp) : hercules_occupancy<1, false>(p.interp));
@@ -203,6 +268,18 @@ bool das_hercules_supported(const DasParams &p)
 	       p.rf_count >= (int64_t)p.C * p.T * p.S && p.loop_end == p.C;
 }
 
+template <int SY, bool H>
+static void launch_staged(const DasParams &q, const float4 *table, cudaStream_t s)
+{
+	using STile = HercTile<SY, 128>;
+	const dim3 grid((q.dims[0] + STile::X - 1) / STile::X, ((q.dims[1] + STile::Y - 1) / STile::Y) * q.groups,
+	                (q.dims[2] + STile::Z * STile::NV - 1) / (STile::Z * STile::NV));
+	if (q.interp == INTERP_CUBIC)
+		das_hercules_staged<INTERP_CUBIC, SY, H><<<grid, 128, stg_smem_bytes<INTERP_CUBIC, SY, H>(), s>>>(q, table);
+	else
+		das_hercules_staged<INTERP_LINEAR, SY, H><<<grid, 128, stg_smem_bytes<INTERP_LINEAR, SY, H>(), s>>>(q, table);
+}
+
 template <int TY, bool H>
 static void launch_hercules_tiles(const DasParams &p, const float4 *table, cudaStream_t s)
 {
@@ -210,6 +287,14 @@ static void launch_hercules_tiles(const DasParams &p, const float4 *table, cudaS
 	using Tile = HercTile<TY, THREADS>;
 	dim3 grid((p.dims[0] + Tile::X - 1) / Tile::X, ((p.dims[1] + Tile::Y - 1) / Tile::Y) * p.groups,
 	          (p.dims[2] + Tile::Z * Tile::NV - 1) / (Tile::Z * Tile::NV));
+	if (use_staged(p)) {
+		DasParams q = p;
+		const char *env = std::getenv("OGL_BF_DAS_STAGED");
+		q.stage_only = env && std::strcmp(env, "require") == 0;
+		if (TY != 1 && staged_volume_ty() == 8) launch_staged<8, H>(q, table, s);
+		else                                    launch_staged<TY, H>(q, table, s);
+		return;
+	}
 	switch (p.interp) {
 	case INTERP_CUBIC:  das_hercules<INTERP_CUBIC, TY, H><<<grid, THREADS, 0, s>>>(p, table); break;
 	case INTERP_LINEAR: das_hercules<INTERP_LINEAR, TY, H><<<grid, THREADS, 0, s>>>(p, table); break;

@@ -118,6 +118,12 @@ struct DasParams {
 	int32_t        half_table;
 	unsigned      *absmax;
 	float          fs_c, toff_fs;
+	/* set to 1 by a kernel whose bounded wait ran out (the staged HERCULES path);
+	 * beamformer_gb300_synchronize reports it */
+	unsigned      *wait_error;
+	/* tests only (OGL_BF_DAS_STAGED=require): blocks of the staged HERCULES kernel
+	 * that cannot stage write NaN instead of running the unstaged code */
+	int32_t        stage_only;
 };
 
 /* Exhaustively compare x * rb + correction with IEEE x / b for every float x in

@@ -721,6 +721,11 @@ bool fill_das_params(const Plan &pl, int kind, const void *rf, uint64_t rf_bytes
 	if (p.rx_step > 1 && (p.family != DAS_HERCULES || !p.fast || p.sparse_mode)) return fail(BF_LIB_ERR_KIND_UNSUPPORTED), false;
 	p.fs_c = (float)((double)p.fs / (double)p.c);
 	p.toff_fs = (float)((double)p.toff * (double)p.fs);
+	if (!g.d_tc_error) {
+		if (!cuda_ok(cudaMalloc(&g.d_tc_error, sizeof(unsigned)))) return false;
+		if (!cuda_ok(cudaMemset(g.d_tc_error, 0, sizeof(unsigned)))) return false;
+	}
+	p.wait_error = g.d_tc_error;
 	p.half_table = g.das_precision == 1 ? 1 : 0;
 	if (p.half_table) {
 		if (!g.d_absmax && !cuda_ok(cudaMalloc(&g.d_absmax, sizeof(unsigned)))) return false;
@@ -1583,7 +1588,7 @@ LIB_FN uint32_t beamformer_gb300_synchronize(int32_t timeout_ms)
 	if (!wait_event(g.last_done, timeout_ms)) return fail(BF_LIB_ERR_KIND_SYNC_VARIABLE);
 	if (!cuda_ok(cudaStreamSynchronize(g.stream))) return 0;
 	if (g.d_tc_error) {
-		/* a tensor-core FIR wait that ran out (the kernel stopped early) */
+		/* a bounded wait that ran out (tensor-core FIR, staged DAS: the kernel stopped early) */
 		unsigned e = 0;
 		if (!cuda_ok(cudaMemcpy(&e, g.d_tc_error, sizeof(e), cudaMemcpyDeviceToHost))) return 0;
 		if (e) {

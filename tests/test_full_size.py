@@ -162,3 +162,44 @@ def test_precision_workload_front_end(precision):
     print(f"precision {precision}: demodulated {e_dem:.1f} dB, plane {e_vol:.1f} dB against FP64")
     assert e_dem <= PRECISION_BOUND[precision], e_dem
     assert e_vol <= PRECISION_BOUND[precision], e_vol
+
+
+def test_volume_workload_every_block_staged(monkeypatch):
+    """The 3D workload's DAS reads every term from shared-memory windows: with
+    OGL_BF_DAS_STAGED=require a block that could not stage would write NaN
+    instead of running the unstaged code. FP32 against the oracle on stratified
+    voxels; the FP16 table (DAS precision 1) against FP32 within -50 dB."""
+    monkeypatch.setenv("OGL_BF_DAS_STAGED", "require")
+    bp = volume_params()
+    bp.output_points[3] = 1
+    pipe = PIPE
+    kaiser = synth.kaiser_spec(64)
+    dims = (128, 128, 256)
+    raw = synth.acquisition(bp, 17, n_points=200, n_speckle=2000, device="cuda")
+    bf = Beamformer().configure(bp, pipe, kaiser=kaiser)
+    vols = {}
+    try:
+        for prec in (0, 1):
+            assert bf.lib.beamformer_gb300_set_das_precision(prec)
+            bf.push(raw)
+            bf.synchronize()
+            vols[prec] = bf.frame(0)[0].copy()
+    finally:
+        bf.lib.beamformer_gb300_set_das_precision(0)
+    assert np.all(np.isfinite(vols[0])) and np.all(np.isfinite(vols[1]))
+    assert nrmse(vols[1], vols[0]) <= -50.0
+    orc = oracle_for(bf, bp, pipe, kaiser=kaiser)
+    orc.shaders = [SH["Decode"], SH["Demodulate"]]
+    front = orc.compute(raw)
+    plan = O.plan(bp, pipe, [0] * len(pipe), abi.DATA_KIND["Int16"],
+                  [(0, kaiser[3], kaiser[2], kaiser[0], kaiser[1]), None, None, None])
+    rf = front["channel_data"][: plan.rf_size // 4]
+    V, per = int(np.prod(dims)), 256
+    out = np.zeros(2 * V, np.float32)
+    got, exp = [], []
+    for i in range(8):
+        v0 = (V // 8) * i + 4096 * (i % 4)
+        O.das(plan.das, rf, dims, orc.sparse, orc.focal, fast=True, voxel_begin=v0, voxel_end=v0 + per, out=out)
+        got.append(vols[0][2 * v0: 2 * (v0 + per)])
+        exp.append(out[2 * v0: 2 * (v0 + per)].copy())
+    check_volume(np.concatenate(got), np.concatenate(exp), "3D workload, staged blocks only")
