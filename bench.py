@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-variants", action="store_true",
+                    help="skip the precision and batched variants that the default line carries")
     ap.add_argument("--speckle", type=int, default=N_SPECKLE)
     ap.add_argument("--profile-frames", type=int, default=0,
                     help="only push this many copies of one device-resident frame through the pipeline "
@@ -516,7 +518,11 @@ def _events_ms(fn, stream, reps):
     return e0.elapsed_time(e1) / reps
 
 
-def run_precision(args, peaks):
+PRECISION_WORKLOAD = ("HERCULES plane 128x1x128, 128 tx, 128 rx, 4096 int16 samples, 128-tap Kaiser, decimation 2, "
+                      "linear DAS")
+
+
+def precision_summary(args):
     """Precision variant on its workload: HERCULES plane 128 x 128, 4096 int16
     samples, 128-tap FIR, decimation 2, linear DAS; frames/s of the whole
     pipeline per arithmetic and each stage's error against the FP64 oracle."""
@@ -571,19 +577,23 @@ def run_precision(args, peaks):
     for v in res.values():
         for k in ("channel_data", "frame", "bf"):
             v.pop(k)
+    return {"workload": PRECISION_WORKLOAD, "per_precision": res, "errors_vs_fp64": errors,
+            "speedup_vs_fp32": {k: res[k]["frames_per_s"] / res["fp32"]["frames_per_s"] for k in res}}
+
+
+def run_precision(args, peaks):
+    sm = precision_summary(args)
     vol3d = _precision_volume(args)
     print(json.dumps({
         "metric": "frames/s of the precision variant (decode + demodulate + DAS, plane)", "variant": "precision",
-        "value": res["bf16"]["frames_per_s"], "unit": "frames/s", "n_gpus": 1, "steps": args.steps,
+        "value": sm["per_precision"]["bf16"]["frames_per_s"], "unit": "frames/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "higher_is_better": True,
         "dtype": "fp16/bf16 front-end operands, fp16 DAS table, f32 accumulate",
         "data": "synthetic (seeded RF generator)",
-        "config": {"workload": "HERCULES plane 128x1x128, 128 tx, 128 rx, 4096 int16 samples, 128-tap Kaiser, "
-                               "decimation 2, linear DAS", "l2": "one 134 MB frame per push, larger than L2",
+        "config": {"workload": PRECISION_WORKLOAD, "l2": "one 134 MB frame per push, larger than L2",
                    "das_precision": "1 (fp16 table) for fp16 and bf16, 0 for fp32"},
-        "per_precision": res, "errors": errors,
-        "speedup_vs_fp32": {k: res[k]["frames_per_s"] / res["fp32"]["frames_per_s"] for k in res},
-        "volume_3d": vol3d}))
+        "per_precision": sm["per_precision"], "errors": sm["errors_vs_fp64"],
+        "speedup_vs_fp32": sm["speedup_vs_fp32"], "volume_3d": vol3d}))
     return 0
 
 
@@ -666,7 +676,7 @@ def _batch_case(args, params, seed0, interp):
     return ms_batch, ms_single, launches, tuning, build_s
 
 
-def run_batched(args, peaks):
+def batched_summary(args):
     """Batched variant: 32 seeded acquisitions (transmits {32, 64, 128}, samples
     {1024, 2048, 4096}, grids from 64x64 planes to 128x128x256 volumes,
     HERCULES or FORCES), cubic DAS, beamformed by one batch call (graph replay)
@@ -682,16 +692,12 @@ def run_batched(args, peaks):
                                  grids=((64, 1, 64), (128, 1, 128)), interpolate=1)
     sm_batch, sm_single, sm_launches, _, sm_build = _batch_case(args, small, 900, 1)
     vox = [int(np.prod(list(bp.output_points)[:3])) for bp in params]
-    reps = max(args.steps, 1)
-    print(json.dumps({
-        "metric": "volumes/s of 32 mixed acquisitions, batched vs one at a time", "variant": "batched",
-        "value": 32 / (ms_batch / 1e3), "unit": "volumes/s", "n_gpus": 1, "steps": reps, "warmup": args.warmup,
-        "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded RF generator)",
-        "config": {"workload": "32 acquisitions: transmits {32,64,128}, samples {1024,2048,4096}, grids "
-                               "{64x1x64, 128x1x128, 64x64x128, 128x128x256}, HERCULES or FORCES, 128 rx, cubic DAS",
-                   "acquisitions": [{"T": int(bp.dec_data_dim[2]), "S": int(bp.dec_data_dim[0]),
-                                     "grid": list(bp.output_points)[:3], "das": int(bp.das_shader_id)} for bp in params],
-                   "total_voxels": int(sum(vox))},
+    return {
+        "workload": "32 acquisitions: transmits {32,64,128}, samples {1024,2048,4096}, grids "
+                    "{64x1x64, 128x1x128, 64x64x128, 128x128x256}, HERCULES or FORCES, 128 rx, cubic DAS",
+        "acquisitions": [{"T": int(bp.dec_data_dim[2]), "S": int(bp.dec_data_dim[0]),
+                          "grid": list(bp.output_points)[:3], "das": int(bp.das_shader_id)} for bp in params],
+        "total_voxels": int(sum(vox)), "volumes_per_s": 32 / (ms_batch / 1e3),
         "ms_per_batch": ms_batch, "gpu_launches_per_batch": launches,
         "one_at_a_time": {"ms_per_batch": ms_single, "volumes_per_s": 32 / (ms_single / 1e3),
                           "how": "configure + push_device per acquisition (the plain API), host-timed"},
@@ -702,7 +708,19 @@ def run_batched(args, peaks):
                                      "128x1x128}, HERCULES or FORCES, 128 rx, cubic DAS",
                          "ms_per_batch": sm_batch, "gpu_launches_per_batch": sm_launches,
                          "one_at_a_time_ms": sm_single, "speedup_vs_one_at_a_time": sm_single / sm_batch,
-                         "first_call_s": sm_build}}))
+                         "first_call_s": sm_build}}
+
+
+def run_batched(args, peaks):
+    sm = batched_summary(args)
+    reps = max(args.steps, 1)
+    line = {"metric": "volumes/s of 32 mixed acquisitions, batched vs one at a time", "variant": "batched",
+            "value": sm["volumes_per_s"], "unit": "volumes/s", "n_gpus": 1, "steps": reps, "warmup": args.warmup,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded RF generator)",
+            "config": {"workload": sm.pop("workload"), "acquisitions": sm.pop("acquisitions"),
+                       "total_voxels": sm.pop("total_voxels")}}
+    line.update(sm)
+    print(json.dumps(line))
     return 0
 
 
@@ -894,6 +912,15 @@ def main():
         line["mixed_precision"] = m
     if r.get("plane"):
         line["plane_workload"] = r["plane"]
+    if world == 1 and not args.no_variants:
+        # the precision and batched variants on their own workloads, measured in the
+        # same run (a failure is reported here instead of losing the headline line)
+        line["variants"] = {}
+        for name, fn in (("precision", precision_summary), ("batched", batched_summary)):
+            try:
+                line["variants"][name] = fn(args)
+            except Exception as exc:                       # noqa: BLE001
+                line["variants"][name] = {"error": f"{type(exc).__name__}: {exc}"}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample()
         if r.get("plane"):

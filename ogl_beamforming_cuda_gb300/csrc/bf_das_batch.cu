@@ -11,8 +11,8 @@
  * by value in the kernel's parameter space (up to DAS_BATCH_MAX per launch), so a
  * tile reads them through the constant cache as a single launch does, and runs
  * the same per-tile code as the single-acquisition kernels: the HERCULES fast
- * path (bf_das_hercules.cuh) with volume or plane tiles, or the general path
- * (bf_das_generic.cuh) for FORCES. The two paths are two persistent launches
+ * path (bf_das_hercules.cuh) with volume or plane tiles, or for FORCES the fast
+ * path (bf_das_forces.cuh; the general path for nearest interpolation). The two paths are two persistent launches
  * with their own work lists, so each keeps its own register budget.
  * Every voxel of every acquisition is written once, in the same arithmetic and
  * accumulation order as the single-acquisition launch.
@@ -21,6 +21,7 @@
 #include "bf_das_math.cuh"
 #include "bf_das_generic.cuh"
 #include "bf_das_hercules.cuh"
+#include "bf_das_forces.cuh"
 
 namespace bf {
 
@@ -52,7 +53,11 @@ das_batch(const __grid_constant__ DasBatchArgs args, const int4 *__restrict__ it
 			 * through a runtime-indexed parameter load per use */
 			const DasParams p = a.p;
 			if (vx < p.dims[0] && vz < p.dims[2]) {
-				const float2 v = das_voxel<DAS_FORCES, INTERP, true>(p, vx, vy, vz, 0, p.loop_end);
+				/* acquisitions with a table take the FORCES fast path */
+				const float2 v = INTERP != INTERP_NEAREST && a.table
+				                     ? forces_voxel<INTERP == INTERP_NEAREST ? INTERP_CUBIC : INTERP>(p, a.table, vx, vy, vz,
+				                                                                                     0, p.loop_end)
+				                     : das_voxel<DAS_FORCES, INTERP, true>(p, vx, vy, vz, 0, p.loop_end);
 				p.frame[((int64_t)vz * p.dims[1] + vy) * p.dims[0] + vx] = v;
 			}
 		}

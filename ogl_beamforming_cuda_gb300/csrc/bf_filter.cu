@@ -21,8 +21,9 @@
  *
  * fir_reg<L, D, R, DEMOD> (the float kinds, taps padded to L in {16, 32, 64, 128},
  * decimation D in {1, 2, 4}): a block of 64 threads owns 64 * R consecutive
- * outputs of one row. The rotated input window is staged once in shared memory,
- * transposed so that the lanes' reads are conflict free. Each thread makes R = 8
+ * outputs of one row. The rotated input window is staged once in shared memory as
+ * pairs of consecutive inputs, transposed so that the lanes' 16-byte reads (two
+ * inputs each) are conflict free. Each thread makes R = 8
  * consecutive outputs in one fully unrolled pass over its (R - 1) D + L window
  * inputs: every staged input is read once per thread, and the taps travel by
  * value in the kernel's parameter space, so each product is one FMA with its tap
@@ -146,9 +147,13 @@ fir_reg(FilterParams p, const __grid_constant__ FirTaps taps)
 {
 	constexpr int NB = FIRR_THREADS * R;          /* outputs per block */
 	constexpr int RD = R * D;
+	constexpr int HD = RD / 2;                    /* input pairs per thread step */
 	constexpr int WIN = NB * D + L;               /* inputs j in [n0 D - L, (n0 + NB) D) */
-	constexpr int S = ((WIN + RD - 1) / RD + 1) | 1;
-	__shared__ float2 w[RD * S];
+	/* input pairs (m, m + 1), m even, as float4: pair P at [(P % HD) S + P / HD]; the odd
+	 * stride keeps the staging stores and the lanes' LDS.128 reads conflict free */
+	constexpr int S = ((WIN / 2 + HD - 1) / HD + 1) | 1;
+	static_assert(RD % 2 == 0, "pairs of inputs per thread step");
+	__shared__ float4 w[HD * S];
 
 	const uint32_t c = blockIdx.y, t = blockIdx.z;
 	const int64_t n0 = (int64_t)blockIdx.x * NB;
@@ -182,25 +187,33 @@ fir_reg(FilterParams p, const __grid_constant__ FirTaps taps)
 				const float x0 = x.x, y0 = -x.y;
 				x = make_float2(1.41421356f * (ph[k].x * x0 + ph[k].y * y0), 1.41421356f * (ph[k].x * y0 - ph[k].y * x0));
 			}
-			w[(q % RD) * S + q / RD] = x;
+			const int P = q / 2;
+			((float2 *)w)[2 * ((P % HD) * S + P / HD) + (q & 1)] = x;
 		}
 	}
 	__syncthreads();
 
-	/* output n0 + th R + r reads inputs e = th R D + r D + k, k < L, with tap h[L - 1 - k] */
+	/* output n0 + th R + r reads inputs e = th R D + r D + k, k < L, with tap h[L - 1 - k];
+	 * one LDS.128 brings inputs 2 i2 and 2 i2 + 1 (the window's last pair may hold one
+	 * input past the taps, which no output uses) */
 	const int th = threadIdx.x;
 	float2 acc[R];
 	#pragma unroll
 	for (int r = 0; r < R; r++) acc[r] = make_float2(0.0f, 0.0f);
 	#pragma unroll
-	for (int i = 0; i < (R - 1) * D + L; i++) {
-		const float2 x = w[(i % RD) * S + th + i / RD];
+	for (int i2 = 0; i2 < ((R - 1) * D + L + 1) / 2; i2++) {
+		const float4 xx = w[(i2 % HD) * S + th + i2 / HD];
 		#pragma unroll
-		for (int r = 0; r < R; r++) {
-			const int k = i - r * D;
-			if (k >= 0 && k < L) {
-				acc[r].x = fmaf(x.x, taps.h[L - 1 - k], acc[r].x);
-				acc[r].y = fmaf(x.y, taps.h[L - 1 - k], acc[r].y);
+		for (int h = 0; h < 2; h++) {
+			const int i = 2 * i2 + h;
+			const float2 x = h ? make_float2(xx.z, xx.w) : make_float2(xx.x, xx.y);
+			#pragma unroll
+			for (int r = 0; r < R; r++) {
+				const int k = i - r * D;
+				if (k >= 0 && k < L) {
+					acc[r].x = fmaf(x.x, taps.h[L - 1 - k], acc[r].x);
+					acc[r].y = fmaf(x.y, taps.h[L - 1 - k], acc[r].y);
+				}
 			}
 		}
 	}

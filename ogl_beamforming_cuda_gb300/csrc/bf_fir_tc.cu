@@ -24,8 +24,9 @@
  * Per block: one thread waits for the block's atoms, issues 4 (1 + E / 64)
  * tcgen05.mma (M = 128, N = 2B, K = 16, fp16/bf16 operands, FP32 accumulate in
  * tensor memory, double-buffered columns) and commits to an mbarrier; all four
- * warps read their 32 accumulator lanes with tcgen05.ld, rotate by e^{i theta n D}
- * and store complex f32 [row][n]. The next block's MMAs are issued before the
+ * warps read their 32 accumulator lanes with tcgen05.ld, rotate by e^{i theta n D},
+ * stage the rows in a padded shared-memory tile and store complex f32 [row][n] as
+ * whole row segments (16 bytes per lane, coalesced). The next block's MMAs are issued before the
  * epilogue of the current one. Every wait is bounded (about one second); a wait
  * that runs out sets the error word and the CTA stops after draining its loads.
  */
@@ -60,6 +61,7 @@ struct FirTcParams {
 	unsigned     *error;        /* set to 1 when a wait runs out */
 	long long     stall_cycles; /* > 0 (tests only): the first wait is on a barrier nothing
 	                               arrives at, bounded by this many cycles, so it runs out */
+	int32_t       vec_store;    /* rows start 16-byte aligned (n_out even): 16-byte stores */
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -165,6 +167,7 @@ fir_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtenso
 	uint8_t *ring = smem;                                        /* TC_RING atoms */
 	uint8_t *gsm  = ring + TC_RING * TC_ATOM_BYTES;              /* atoms x (N rows x 128 B) */
 	uint64_t *bars = (uint64_t *)(gsm + (size_t)p.atoms * N * 128);
+	float4 *epi = (float4 *)(bars + TC_RING + 4);              /* 4 warps x 32 rows x (N / 4 + 1) chunks */
 	__shared__ uint32_t tmem_slot;
 	__shared__ int stop;
 
@@ -248,20 +251,38 @@ fir_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtenso
 				tmem_ld32(ta, v);
 				if (N == 64) tmem_ld32(ta + 32, v + 32);
 			}
-			const int row = row0 + warp * 32 + lane;
+			/* rotate this lane's row into the warp's staging tile (row = lane, 16-byte
+			 * chunks of two outputs, rows padded by one chunk: conflict-free both ways),
+			 * then store whole row segments: CPR lanes per row, 32 / CPR rows per
+			 * instruction, 16 bytes per lane (coalesced) */
+			constexpr int CPR = B / 2;
+			float4 *tile = epi + warp * 32 * (CPR + 1);
 			const int nb = (q0 + i) * B;
-			if (row < p.rows) {
-				float2 *o = p.out + (size_t)row * p.n_out;
-				#pragma unroll
-				for (int j = 0; j < B; j++) {
-					const int n = nb + j;
-					if (n < p.n_out) {
-						const float2 r = __ldg(p.rot + n);
-						const float zr = v[j], zi = v[B + j];
-						o[n] = make_float2(zr * r.x - zi * r.y, zr * r.y + zi * r.x);
+			#pragma unroll
+			for (int j = 0; j < B; j += 2) {
+				const int n = nb + j;
+				const float2 r0 = __ldg(p.rot + min(n, p.n_out - 1)), r1 = __ldg(p.rot + min(n + 1, p.n_out - 1));
+				const float a = v[j], b = v[B + j], c = v[j + 1], d = v[B + j + 1];
+				tile[lane * (CPR + 1) + j / 2] =
+				    make_float4(a * r0.x - b * r0.y, a * r0.y + b * r0.x, c * r1.x - d * r1.y, c * r1.y + d * r1.x);
+			}
+			__syncwarp();
+			#pragma unroll
+			for (int k = 0; k < 32; k += 32 / CPR) {
+				const int rl = k + lane / CPR, ch = lane % CPR;
+				const int row = row0 + warp * 32 + rl, n = nb + 2 * ch;
+				const float4 y = tile[rl * (CPR + 1) + ch];
+				if (row < p.rows && n < p.n_out) {
+					float2 *o = p.out + (size_t)row * p.n_out + n;
+					if (p.vec_store && n + 1 < p.n_out) {
+						*(float4 *)o = y;
+					} else {
+						o[0] = make_float2(y.x, y.y);
+						if (n + 1 < p.n_out) o[1] = make_float2(y.z, y.w);
 					}
 				}
 			}
+			__syncwarp();
 		} else {
 			stop = 1;
 		}
@@ -409,15 +430,20 @@ cudaError_t launch_fir_tc(const void *x, uint32_t rows, uint32_t row_samples, ui
 	int splits = (4 * device_sm_count() + row_blocks - 1) / row_blocks;
 	splits = std::min(splits, std::max(1, p.q_blocks / 4));
 	p.splits = splits;
-	const size_t smem = 1024 + (size_t)TC_RING * TC_ATOM_BYTES + (size_t)p.atoms * N * 128 + (TC_RING + 4) * 8;
-	static bool attr = false;
-	if (!attr) {
-		cudaFuncSetAttribute(fir_tc<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-		cudaFuncSetAttribute(fir_tc<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-		cudaFuncSetAttribute(fir_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-		attr = true;
-	}
-	if (smem > 200 * 1024) return cudaErrorInvalidValue;
+	p.vec_store = (n_out % 2 == 0 && ((uintptr_t)out & 15) == 0) ? 1 : 0;
+	const size_t smem = 1024 + (size_t)TC_RING * TC_ATOM_BYTES + (size_t)p.atoms * N * 128 + (TC_RING + 4) * 8 +
+	                    (size_t)4 * 32 * (N / 4 + 1) * 16;
+	/* the dynamic shared memory this launch needs, within the device's opt-in limit
+	 * less the kernel's static shared memory */
+	int dev = 0, optin = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+	if (e != cudaSuccess) return e;
+	const void *fn = N == 16 ? (const void *)fir_tc<16> : N == 32 ? (const void *)fir_tc<32> : (const void *)fir_tc<64>;
+	cudaFuncAttributes fa{};
+	if ((e = cudaFuncGetAttributes(&fa, fn)) != cudaSuccess) return e;
+	if (smem + fa.sharedSizeBytes > (size_t)optin) return cudaErrorInvalidValue;
+	if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess) return e;
 	const int grid = row_blocks * splits;
 	switch (N) {
 	case 16: fir_tc<16><<<grid, 128, smem, s>>>(xmap, gmap, p); break;

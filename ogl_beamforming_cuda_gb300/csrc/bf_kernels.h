@@ -156,6 +156,10 @@ int64_t     das_hercules_tiles(const DasParams &p);
 int         das_hercules_blocks_per_sm(const DasParams &p);
 int64_t     das_hercules_table_bytes(const DasParams &p);
 cudaError_t launch_das_hercules(const DasParams &p, float4 *table, cudaStream_t s);
+/* FORCES fast path (bf_das_forces.cu): the same per-frame table (das_hercules_table_bytes
+ * bytes, built by the launch), for parameters das_forces_supported accepts */
+bool        das_forces_supported(const DasParams &p);
+cudaError_t launch_das_forces(const DasParams &p, float4 *table, cudaStream_t s);
 cudaError_t launch_sum(float2 *out, const float2 *const *ins, int count, float prescale, const int32_t dims[3],
                        cudaStream_t s);
 cudaError_t launch_min_max(const float2 *level0, const int32_t dims[3], int mips, float2 *levels, cudaStream_t s);

@@ -726,7 +726,7 @@ bool fill_das_params(const Plan &pl, int kind, const void *rf, uint64_t rf_bytes
 		if (!cuda_ok(cudaMemset(g.d_tc_error, 0, sizeof(unsigned)))) return false;
 	}
 	p.wait_error = g.d_tc_error;
-	p.half_table = g.das_precision == 1 ? 1 : 0;
+	p.half_table = g.das_precision == 1 && p.family == DAS_HERCULES ? 1 : 0;
 	if (p.half_table) {
 		if (!g.d_absmax && !cuda_ok(cudaMalloc(&g.d_absmax, sizeof(unsigned)))) return false;
 		p.absmax = g.d_absmax;
@@ -862,7 +862,8 @@ bool run_stage(int i, const void *src, uint64_t src_bytes, DeviceFrame &frame, b
 		}
 		/* OGL_BF_DAS_GENERIC=1 keeps every DAS on das_kernel (for comparisons) */
 		const char *generic = std::getenv("OGL_BF_DAS_GENERIC");
-		if (das_hercules_supported(p) && !(generic && generic[0] == '1')) {
+		const bool herc = das_hercules_supported(p), forces = das_forces_supported(p);
+		if ((herc || forces) && !(generic && generic[0] == '1')) {
 			const uint64_t need = (uint64_t)das_hercules_table_bytes(p);
 			if (need > g.das_table_bytes) {
 				cudaStreamSynchronize(g.stream);
@@ -872,7 +873,7 @@ bool run_stage(int i, const void *src, uint64_t src_bytes, DeviceFrame &frame, b
 				if (!cuda_ok(cudaMalloc(&g.das_table, need))) return false;
 				g.das_table_bytes = need;
 			}
-			err = launch_das_hercules(p, g.das_table, g.stream);
+			err = herc ? launch_das_hercules(p, g.das_table, g.stream) : launch_das_forces(p, g.das_table, g.stream);
 		} else {
 			err = launch_das(p, g.stream);
 		}
@@ -1170,7 +1171,7 @@ cudaError_t batch_launch(cudaStream_t s)
 			if (e != cudaSuccess) return e;
 			last = out_idx;
 		}
-		if (a.path != DAS_BATCH_GENERIC && das_hercules_table_bytes(a.das) > 0) {
+		if (a.das_table && das_hercules_table_bytes(a.das) > 0) {
 			const cudaError_t e = launch_das_table(a.das, a.das_table, s);
 			if (e != cudaSuccess) return e;
 		}
@@ -1289,6 +1290,10 @@ bool build_batch(const BeamformerParameters *params, uint32_t count, const void 
 			}
 		} else if (a.das.family == DAS_FORCES && !a.das.sparse_mode) {
 			a.path = DAS_BATCH_GENERIC;
+			if (das_forces_supported(a.das)) {
+				/* the FORCES fast path reads the same per-frame table */
+				if (!cuda_ok(cudaMalloc(&a.das_table, (size_t)das_hercules_table_bytes(a.das)))) return false;
+			}
 		} else {
 			return fail(BF_LIB_ERR_KIND_UNSUPPORTED), false;
 		}

@@ -284,3 +284,25 @@ def test_das_rotated_scaled_transducer_transform(monkeypatch, z_deg, scale, x_de
     bf, ref = run_both(bp, [SH["Decode"], SH["Demodulate"], shader], raw, interpolation=interp)
     assert np.any(ref["frame"] != 0)
     check_volume(bf.frame(0)[0], ref["frame"], f"{kernel} xdc rot z {z_deg} x {x_deg} scale {scale} interp={interp}")
+
+
+@pytest.mark.parametrize("interp", (1, 2))
+@pytest.mark.parametrize("points", ((48, 1, 64), (16, 6, 32)))
+@pytest.mark.parametrize("fc_scale", (1.0, 2.0))
+def test_das_forces_fast_path(interp, points, fc_scale):
+    """FORCES through the fast path (per-frame table, proven voxels; the rest on
+    the general per-voxel code), deep enough that most voxels carry the proof,
+    both demodulation phase paths (theta = 2 pi and 4 pi), against the oracle."""
+    bp = small_params(S=1024, C=32, T=32, points=points, das="FORCES")
+    bp.center_frequency *= fc_scale
+    raw = small_raw(bp, n_points=12, n_speckle=200)
+    bf, ref = run_both(bp, [SH["Decode"], SH["Demodulate"], SH["DAS"]], raw, interpolation=interp)
+    check_volume(bf.frame(0)[0], ref["frame"], f"FORCES fast path interp={interp} {points} fc x {fc_scale}")
+
+
+@pytest.mark.parametrize("interp", (1, 2))
+def test_das_forces_fast_path_without_demodulation(interp):
+    bp = small_params(S=512, C=16, T=16, points=(24, 2, 40), D=1, das="FORCES")
+    raw = small_raw(bp)
+    bf, ref = run_both(bp, [SH["Decode"], SH["DAS"]], raw, kaiser=None, interpolation=interp)
+    check_volume(bf.frame(0)[0], ref["frame"], f"FORCES fast path, no demodulation, interp={interp}")
