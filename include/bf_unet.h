@@ -25,10 +25,17 @@ extern "C" {
 #define BF_UNET_BF16 1
 
 /* out[co] = relu?(bias[co] + sum_ci w[co][ci] * in[ci]) + residual[co] (residual
- * optional, same type as out, may alias nothing else). */
+ * optional, same type as out, may alias nothing else). BF16 inputs run as an
+ * implicit GEMM on the tensor cores (tcgen05, FP32 accumulation); FP32 inputs on
+ * the direct kernel. Calls on one stream share a weight staging buffer: do not
+ * run two on different streams at once. */
 uint32_t bf_unet_conv3d(const void *in, int32_t in_type, int32_t cin, const uint16_t *w, const float *bias,
                         const void *residual, void *out, int32_t out_type, int32_t cout, const int32_t dims[3],
                         int32_t relu, void *stream);
+
+/* Nonzero when a tensor-core convolution's bounded wait ran out since the last
+ * call (its CTA stopped early); synchronises `stream` first and clears the flag. */
+uint32_t bf_unet_tc_errors(void *stream);
 
 /* grad_in[ci] = sum_co w[co][ci] (flipped) * grad_out[co]; w_scratch holds
  * cin * cout * 27 bf16 (the transposed, flipped weights). */

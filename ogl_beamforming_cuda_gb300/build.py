@@ -22,7 +22,7 @@ NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 INC = [f"-I{os.path.join(ROOT, 'include')}", f"-I{CSRC}"]
 
-CU = ["bf_decode.cu", "bf_filter.cu", "bf_fir_tc.cu", "bf_das.cu", "bf_das_hercules.cu", "bf_das_forces.cu", "bf_das_batch.cu", "bf_reduce.cu", "bf_hilbert.cu", "bf_unet.cu"]
+CU = ["bf_decode.cu", "bf_filter.cu", "bf_fir_tc.cu", "bf_das.cu", "bf_das_hercules.cu", "bf_das_forces.cu", "bf_das_batch.cu", "bf_reduce.cu", "bf_hilbert.cu", "bf_unet.cu", "bf_unet_tc.cu"]
 CPP = ["bf_host.cpp", "bf_library.cpp", "bf_server.cpp"]
 HEADERS = ["bf_kernels.h", "bf_host.h", "bf_das_math.cuh", "bf_das_generic.cuh", "bf_das_hercules.cuh", "bf_das_staged.cuh", "bf_das_forces.cuh"]
 

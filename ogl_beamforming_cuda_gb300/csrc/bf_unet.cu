@@ -4,7 +4,9 @@
  * pooling and upsampling, the ReLU derivative, the MSE loss, Adam, and the
  * seeded RF synthesis that makes the training data.
  *
- * Convolution forward (direct, channels-first): a block computes an 8 x 8 x 32
+ * Convolution forward of BF16 inputs: bf_unet_tc.cu (tcgen05 implicit GEMM).
+ * Convolution forward of FP32 inputs (the input gradient; OGL_BF_UNET_SIMT=1 for
+ * every input) here (direct, channels-first): a block computes an 8 x 8 x 32
  * output tile for 8 output channels. Per input channel it stages the tile with
  * its one-voxel halo (10 x 10 x 34 values, FP32) and the 27 x 8 taps in shared
  * memory; each thread owns one (y, x) column of 8 depths, loads the 10 input
@@ -374,6 +376,12 @@ int grid_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, (int64_
 } /* namespace */
 } /* namespace bf */
 
+namespace bf {
+/* bf_unet_tc.cu: the tensor-core form of the forward convolution for BF16 inputs */
+bool conv3d_tc_launch(const void *in, int cin, const uint16_t *w, const float *bias, const void *residual, void *out,
+                      int out_type, int cout, const int32_t dims[3], int relu, cudaStream_t s, cudaError_t &err);
+}
+
 using namespace bf;
 
 #define BF_OK(e) ((e) == cudaSuccess ? 1u : 0u)
@@ -386,6 +394,10 @@ uint32_t bf_unet_conv3d(const void *in, int32_t in_type, int32_t cin, const uint
 {
 	if (!in || !w || !out || cin <= 0 || cout <= 0 || !dims || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return 0;
 	cudaStream_t s = (cudaStream_t)stream;
+	if (in_type == BF_UNET_BF16) {
+		cudaError_t e = cudaSuccess;
+		if (conv3d_tc_launch(in, cin, w, bias, residual, out, out_type, cout, dims, relu, s, e)) return BF_OK(e);
+	}
 	const int W = dims[0], H = dims[1], D = dims[2];
 	dim3 grid(((W + CX - 1) / CX) * ((H + CY - 1) / CY) * ((D + CZ - 1) / CZ), (cout + COB - 1) / COB);
 	const __nv_bfloat16 *wb = (const __nv_bfloat16 *)w;

@@ -103,6 +103,7 @@ def _bind(lib):
         "bf_unet_adam": [vp, vp, vp, vp, vp, i64, f32, f32, f32, f32, i32, vp],
         "bf_unet_convert": [vp, i32, vp, i32, i64, f32, vp],
         "bf_synth_traces": [vp, vp, i32, vp, i32, i32, i32, f32, f32, f32, f32, f32, vp],
+        "bf_unet_tc_errors": [vp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

@@ -52,6 +52,32 @@ def test_conv_forward(k, cin, cout, dims, relu):
     assert rel(out.cpu().numpy(), ref) < 2e-6
 
 
+@pytest.mark.parametrize("cin,cout,dims,out_type", [(96, 32, (24, 12, 10), torch.bfloat16),
+                                                    (64, 64, (20, 9, 7), torch.float32),
+                                                    (48, 16, (33, 5, 6), torch.bfloat16)])
+def test_conv_forward_tensor_cores_against_direct(k, monkeypatch, cin, cout, dims, out_type):
+    """BF16 inputs run as a tcgen05 implicit GEMM: the wide layers of the network,
+    voxel counts that are not a multiple of the 128-voxel tile, against the direct
+    FP32 kernel (OGL_BF_UNET_SIMT=1) and the float64 restatement; no bounded wait
+    runs out."""
+    rng = np.random.default_rng(cin + cout)
+    W, H, D = dims
+    x = bf16(rng.standard_normal((cin, D, H, W)))
+    w = bf16(rng.standard_normal((cout, cin, 27)) * 0.05)
+    b = rng.standard_normal(cout).astype(np.float32)
+    outs = []
+    for simt in ("0", "1"):
+        monkeypatch.setenv("OGL_BF_UNET_SIMT", simt)
+        out = torch.empty((cout, D, H, W), dtype=out_type, device="cuda")
+        k.conv(dev(x, torch.bfloat16), cin, dev(w.ravel(), torch.bfloat16), dev(b, torch.float32), out, cout, dims, True)
+        outs.append(out.float().cpu().numpy())
+    assert k.lib.bf_unet_tc_errors(k.stream) == 0
+    ref = U.conv3d(x, w, b, relu=True)
+    tol = 2e-6 if out_type == torch.float32 else 8e-3         # BF16 outputs keep 8 significant bits
+    assert rel(outs[0], ref) < tol
+    assert rel(outs[1], ref) < tol
+
+
 def test_conv_grad_input(k):
     rng = np.random.default_rng(7)
     cin, cout, dims = 12, 9, (33, 10, 11)
