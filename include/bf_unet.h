@@ -27,8 +27,8 @@ extern "C" {
 /* out[co] = relu?(bias[co] + sum_ci w[co][ci] * in[ci]) + residual[co] (residual
  * optional, same type as out, may alias nothing else). BF16 inputs run as an
  * implicit GEMM on the tensor cores (tcgen05, FP32 accumulation); FP32 inputs on
- * the direct kernel. Calls on one stream share a weight staging buffer: do not
- * run two on different streams at once. */
+ * the direct kernel (FP32 products). Tensor-core calls share staging buffers
+ * (weights, channels-last input): do not run two on different streams at once. */
 uint32_t bf_unet_conv3d(const void *in, int32_t in_type, int32_t cin, const uint16_t *w, const float *bias,
                         const void *residual, void *out, int32_t out_type, int32_t cout, const int32_t dims[3],
                         int32_t relu, void *stream);
@@ -38,7 +38,10 @@ uint32_t bf_unet_conv3d(const void *in, int32_t in_type, int32_t cin, const uint
 uint32_t bf_unet_tc_errors(void *stream);
 
 /* grad_in[ci] = sum_co w[co][ci] (flipped) * grad_out[co]; w_scratch holds
- * cin * cout * 27 bf16 (the transposed, flipped weights). */
+ * cin * cout * 27 bf16 (the transposed, flipped weights). On volumes whose rows
+ * tile by 128 voxels (W a divisor of 128 and H a multiple of 128 / W, or W a
+ * multiple of 128) grad_out is rounded to BF16 and the sum runs on the tensor
+ * cores with FP32 accumulation; otherwise FP32 products on the direct kernel. */
 uint32_t bf_unet_conv3d_grad_input(const float *grad_out, int32_t cout, const uint16_t *w, float *grad_in, int32_t cin,
                                    const int32_t dims[3], uint16_t *w_scratch, void *stream);
 
@@ -71,6 +74,10 @@ uint32_t bf_unet_mse(const float *y, const float *t, float *grad, float *loss, i
  * copy w16 used by the convolutions */
 uint32_t bf_unet_adam(float *w, const float *grad, float *m, float *v, uint16_t *w16, int64_t n, float lr,
                       float beta1, float beta2, float eps, int32_t step, void *stream);
+
+/* exponential moving average of the master weights: ema = decay ema + (1 - decay) w;
+ * writes the BF16 copy ema16 when it is not null */
+uint32_t bf_unet_ema(float *ema, const float *w, uint16_t *ema16, int64_t n, float decay, void *stream);
 
 /* type conversion (n values) */
 uint32_t bf_unet_convert(const void *x, int32_t x_type, void *y, int32_t y_type, int64_t n, float scale, void *stream);

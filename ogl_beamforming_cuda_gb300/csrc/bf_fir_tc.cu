@@ -38,6 +38,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 namespace bf {
@@ -309,19 +310,20 @@ fir_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtenso
 
 /* ------------------------------------ host ------------------------------------ */
 
-static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+/* the driver's cuTensorMapEncodeTiled (12.0 interface), looked up once; null when
+ * the driver does not provide it */
+void *tensor_map_encoder()
 {
-	static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-	static bool tried = false;
-	if (!tried) {
-		tried = true;
+	static std::once_flag once;
+	static void *fn = nullptr;
+	std::call_once(once, [] {
 		void *f = nullptr;
 		cudaDriverEntryPointQueryResult q;
 		if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
 		    q == cudaDriverEntryPointSuccess)
-			fn = (PFN_cuTensorMapEncodeTiled_v12000)f;
+			fn = f;
 		cudaGetLastError();
-	}
+	});
 	return fn;
 }
 
@@ -330,7 +332,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 static bool make_map(CUtensorMap *m, const void *base, uint64_t cols, uint64_t pitch, uint64_t rows,
                      uint32_t box_rows, bool bf16)
 {
-	PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+	const auto enc = (PFN_cuTensorMapEncodeTiled_v12000)tensor_map_encoder();
 	if (!enc) return false;
 	const cuuint64_t dims[2] = {cols, rows};
 	const cuuint64_t strides[1] = {pitch * 2};

@@ -140,6 +140,8 @@ cudaError_t launch_das(const DasParams &p, cudaStream_t s);
  * accumulate. `table` (fir_tc_table_bytes, device) holds the tap matrix and the
  * per-output rotations written by fir_tc_tables. */
 bool        fir_tc_supported(uint32_t decimation, uint32_t taps);
+/* the driver's cuTensorMapEncodeTiled (PFN_cuTensorMapEncodeTiled_v12000), or null */
+void       *tensor_map_encoder();
 int64_t     fir_tc_table_bytes(uint32_t decimation, uint32_t taps, uint32_t n_out);
 bool        fir_tc_tables(uint32_t decimation, const float *h, uint32_t taps, double demod_frequency,
                           double demod_fs, uint32_t n_out, bool bf16, void *table);

@@ -334,6 +334,16 @@ __global__ void adam_k(float *__restrict__ w, const float *__restrict__ g, float
 	}
 }
 
+__global__ void ema_k(float *__restrict__ e, const float *__restrict__ w, __nv_bfloat16 *__restrict__ e16, int64_t n,
+                      float decay)
+{
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const float ei = decay * e[i] + (1.0f - decay) * w[i];
+		e[i] = ei;
+		if (e16) e16[i] = __float2bfloat16_rn(ei);
+	}
+}
+
 template <typename TI, typename TO>
 __global__ void convert_k(const TI *__restrict__ x, TO *__restrict__ y, int64_t n, float scale)
 {
@@ -378,7 +388,7 @@ int grid_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, (int64_
 
 namespace bf {
 /* bf_unet_tc.cu: the tensor-core form of the forward convolution for BF16 inputs */
-bool conv3d_tc_launch(const void *in, int cin, const uint16_t *w, const float *bias, const void *residual, void *out,
+bool conv3d_tc_launch(const void *in, int in_type, int cin, const uint16_t *w, const float *bias, const void *residual, void *out,
                       int out_type, int cout, const int32_t dims[3], int relu, cudaStream_t s, cudaError_t &err);
 }
 
@@ -396,7 +406,8 @@ uint32_t bf_unet_conv3d(const void *in, int32_t in_type, int32_t cin, const uint
 	cudaStream_t s = (cudaStream_t)stream;
 	if (in_type == BF_UNET_BF16) {
 		cudaError_t e = cudaSuccess;
-		if (conv3d_tc_launch(in, cin, w, bias, residual, out, out_type, cout, dims, relu, s, e)) return BF_OK(e);
+		if (conv3d_tc_launch(in, BF_UNET_BF16, cin, w, bias, residual, out, out_type, cout, dims, relu, s, e))
+			return BF_OK(e);
 	}
 	const int W = dims[0], H = dims[1], D = dims[2];
 	dim3 grid(((W + CX - 1) / CX) * ((H + CY - 1) / CY) * ((D + CZ - 1) / CZ), (cout + COB - 1) / COB);
@@ -426,6 +437,12 @@ uint32_t bf_unet_conv3d_grad_input(const float *grad_out, int32_t cout, const ui
 	                                                               cout, cin);
 	g_kernel_launches++;
 	if (cudaGetLastError() != cudaSuccess) return 0;
+	if (dims && dims[0] > 0 && dims[1] > 0 && dims[2] > 0) {
+		cudaError_t e = cudaSuccess;
+		if (conv3d_tc_launch(grad_out, BF_UNET_F32, cout, w_scratch, nullptr, nullptr, grad_in, BF_UNET_F32, cin, dims, 0,
+		                     s, e))
+			return BF_OK(e);
+	}
 	return bf_unet_conv3d(grad_out, BF_UNET_F32, cout, w_scratch, nullptr, nullptr, grad_in, BF_UNET_F32, cin, dims, 0,
 	                      stream);
 }
@@ -536,6 +553,14 @@ uint32_t bf_unet_adam(float *w, const float *grad, float *m, float *v, uint16_t 
 	const float c1 = 1.0f - powf(beta1, (float)step), c2 = 1.0f - powf(beta2, (float)step);
 	adam_k<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(w, grad, m, v, (__nv_bfloat16 *)w16, n, lr, beta1, beta2, eps,
 	                                                     c1, c2);
+	g_kernel_launches++;
+	return BF_OK(cudaGetLastError());
+}
+
+uint32_t bf_unet_ema(float *ema, const float *w, uint16_t *ema16, int64_t n, float decay, void *stream)
+{
+	if (!ema || !w || n <= 0 || !(decay >= 0.0f && decay <= 1.0f)) return 0;
+	ema_k<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(ema, w, (__nv_bfloat16 *)ema16, n, decay);
 	g_kernel_launches++;
 	return BF_OK(cudaGetLastError());
 }

@@ -26,6 +26,21 @@
  * residual) and stores each output channel's 32 consecutive voxels (coalesced).
  * CTAs are persistent over the voxel tiles.
  *
+ * Two forms share that GEMM:
+ *  - conv3d_tma (volumes whose rows tile by 128 voxels: W a divisor of 128 with
+ *    H a multiple of 128 / W, or W a multiple of 128). The input is first
+ *    rewritten channels-last ([D][H][W][cin_p], cin_p a multiple of 16). One
+ *    K = 16 step is then (tap, 16 input channels), and its A operand is ONE 4D
+ *    TMA box of the channels-last tensor: 16 channels x 128 voxels at the tile's
+ *    origin shifted by the tap, zero-filled outside the volume by the copy engine,
+ *    landing in the 32-byte-swizzled K-major layout that tcgen05 reads. Warp 0
+ *    loads (four boxes and the chunk's weights per stage, a ring of stages), warp
+ *    1 issues the MMAs into one of two tensor-memory accumulators, warps 2-5 read
+ *    the other accumulator and store the previous tile.
+ *  - conv3d_tc (any volume): the threads gather each chunk's A tile from the
+ *    channels-first input, 8 channels per 16-byte group, into 128-byte-swizzled
+ *    rows.
+ *
  * Every wait is bounded (about one second); a wait that runs out sets the error
  * word (bf_unet_tc_errors), the CTA waits (bounded) for its copies and tensor
  * operations in flight, frees its tensor memory and stops.
@@ -33,10 +48,13 @@
 #include "bf_kernels.h"
 #include "bf_unet.h"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 #include <algorithm>
 #include <cstdlib>
+#include <cstring>
 #include <mutex>
 
 namespace bf {
@@ -283,34 +301,378 @@ conv3d_tc(const __grid_constant__ ConvTc p)
 		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(tcols) : "memory");
 }
 
+/* ------------------------------ TMA form ------------------------------ */
+
+constexpr int TS = 4;                    /* stages in the ring */
+constexpr int STEP_A = TCM * 32;         /* one K = 16 step of A: 128 rows x 32 B */
+
+struct ConvTma {
+	const uint8_t *bk;       /* [K step][np rows][32 B], 32-byte swizzled */
+	const float   *bias;
+	const void    *residual;
+	void          *out;
+	int32_t        cout, np, cg, ksteps, nch;   /* cg = cin_p / 16 */
+	int32_t        W, H;
+	int64_t        V;
+	int32_t        relu, tiles;
+	uint32_t       idesc;
+};
+
+/* K-major operand in 32-byte swizzled atoms (8 rows x 32 B, SBO 256 B; the
+ * leading offset is unused when one MMA's K spans one atom), version 1 */
+__device__ __forceinline__ uint64_t sw32(uint32_t addr)
+{
+	uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+	d |= (uint64_t)1 << 16;
+	d |= (uint64_t)(256 >> 4) << 32;
+	d |= (uint64_t)1 << 46;
+	d |= (uint64_t)6 << 61;
+	return d;
+}
+
+/* bounded wait that also gives up when another role of the CTA has given up;
+ * the role whose own wait runs out records the error */
+__device__ __forceinline__ bool wait_role(uint32_t bar, uint32_t parity, volatile int *abort_flag)
+{
+	const long long t0 = clock64();
+	while (true) {
+		uint32_t done;
+		asm volatile("{\n\t.reg .pred p;\n\t"
+		             "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+		             "selp.u32 %0, 1, 0, p;\n\t}"
+		             : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+		if (done) return true;
+		if (*abort_flag) return false;
+		if (clock64() - t0 > TC_WAIT) {
+			*abort_flag = 1;
+			atomicExch(&g_unet_tc_error, 1u);
+			return false;
+		}
+	}
+}
+
+/* B steps: element (n, kk) of K step ks (tap = ks / cg, ci = (ks % cg) * 16 + kk) at
+ * (ks * np + n) * 32 + ((kk / 8) ^ ((n / 4) % 2)) * 16 + (kk % 8) * 2 bytes; zero beyond
+ * cout, cin and the 27 taps */
+__global__ void __launch_bounds__(256)
+prepare_weights_tma(const __nv_bfloat16 *__restrict__ w, uint16_t *__restrict__ bk, int cin, int cg, int cout, int np,
+                    int steps)
+{
+	const int64_t total = (int64_t)steps * np * 16;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+		const int kk = (int)(i & 15);
+		const int64_t r = i >> 4;
+		const int n = (int)(r % np), ks = (int)(r / np);
+		const int tap = ks / cg, ci = (ks - tap * cg) * 16 + kk;
+		uint16_t v = 0;
+		if (n < cout && ci < cin && tap < 27) v = __bfloat16_as_ushort(w[((int64_t)n * cin + ci) * 27 + tap]);
+		bk[((int64_t)ks * np + n) * 16 + ((((kk >> 3) ^ ((n >> 2) & 1))) << 3) + (kk & 7)] = v;
+	}
+}
+
+__device__ __forceinline__ uint32_t bf16_bits(const uint16_t *p, int64_t i) { return __ldg(p + i); }
+__device__ __forceinline__ uint32_t bf16_bits(const float *p, int64_t i)
+{
+	return __bfloat16_as_ushort(__float2bfloat16_rn(__ldg(p + i)));
+}
+
+/* channels-first [cin][V] (BF16, or FP32 rounded to BF16) -> channels-last
+ * [V][cg * 16] BF16 (channels beyond cin are 0); thread per (voxel, 16-channel
+ * block): 16 coalesced loads, one 32-byte store */
+template <typename TI>
+__global__ void __launch_bounds__(256)
+to_channels_last(const TI *__restrict__ in, uint4 *__restrict__ out, int cin, int cg, int64_t V)
+{
+	const int b = blockIdx.y;
+	for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x) {
+		uint32_t w[8];
+		#pragma unroll
+		for (int k = 0; k < 16; k += 2) {
+			const int c0 = b * 16 + k;
+			const uint32_t lo = c0 < cin ? bf16_bits(in, (int64_t)c0 * V + v) : 0u;
+			const uint32_t hi = c0 + 1 < cin ? bf16_bits(in, (int64_t)(c0 + 1) * V + v) : 0u;
+			w[k >> 1] = lo | (hi << 16);
+		}
+		uint4 *o = out + (v * cg + b) * 2;
+		o[0] = make_uint4(w[0], w[1], w[2], w[3]);
+		o[1] = make_uint4(w[4], w[5], w[6], w[7]);
+	}
+}
+
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, int c, int x, int y, int z, uint32_t bar)
+{
+	asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+	             " [%0], [%1, {%2, %3, %4, %5}], [%6];"
+	             :: "r"(dst), "l"((uint64_t)map), "r"(c), "r"(x), "r"(y), "r"(z), "r"(bar) : "memory");
+}
+
+/* 192 threads: warp 0 loads, warp 1 issues the MMAs (and owns tensor memory),
+ * warps 2-5 run the epilogue (warp w reads accumulator lanes 32 (w % 4) ...). */
+template <typename TO>
+__global__ void __launch_bounds__(192)
+conv3d_tma(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ ConvTma p)
+{
+	extern __shared__ uint8_t smem_raw[];
+	uint8_t *sm = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+	const int bstep = p.np * 32, bchunk = 4 * bstep, stage = 4 * STEP_A + bchunk;
+	uint64_t *bars = (uint64_t *)(sm + TS * stage);   /* full[TS], empty[TS], acc_full[2], acc_empty[2] */
+	__shared__ uint32_t tmem_slot;
+	__shared__ int abort_word;
+	volatile int *abort_flag = &abort_word;
+
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const uint32_t full0 = su32(bars), empty0 = full0 + 8 * TS, afull0 = empty0 + 8 * TS, aempty0 = afull0 + 16;
+	const uint32_t tcols = 2 * p.np <= 32 ? 32u : 2 * p.np <= 64 ? 64u : 2 * p.np <= 128 ? 128u : 256u;
+	if (warp == 1) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+		             :: "r"(su32(&tmem_slot)), "r"(tcols) : "memory");
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+	}
+	if (tid == 0) {
+		for (int i = 0; i < 2 * TS + 2; i++)
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(full0 + 8 * i), "r"(1) : "memory");
+		for (int i = 0; i < 2; i++)
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(aempty0 + 8 * i), "r"(4) : "memory");
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+		abort_word = 0;
+		asm volatile("prefetch.tensormap [%0];" :: "l"((uint64_t)&xmap) : "memory");
+	}
+	tc_fence_before();
+	__syncthreads();
+	tc_fence_after();
+	const uint32_t tmem = tmem_slot;
+	const int64_t plane = (int64_t)p.H * p.W;
+	uint32_t issued = 0;                 /* chunks loaded (warp 0, lane 0) */
+	int64_t mma_chunks = 0;              /* chunks whose MMAs were committed (warp 1, lane 0) */
+
+	if (warp == 0) {
+		if (lane == 0) {
+			uint32_t q = 0;
+			for (int tile = blockIdx.x; tile < p.tiles && !*abort_flag; tile += gridDim.x) {
+				const int64_t v0 = (int64_t)tile * TCM;
+				const int x0 = (int)(v0 % p.W), y0 = (int)((v0 / p.W) % p.H), z0 = (int)(v0 / plane);
+				int tap = 0, c16 = 0;
+				for (int c = 0; c < p.nch; c++, q++) {
+					const int s = (int)(q % TS);
+					const uint32_t u = q / TS;
+					if (u > 0 && !wait_role(empty0 + 8 * s, (u - 1) & 1, abort_flag)) break;
+					if (*abort_flag) break;
+					const int steps = min(4, p.ksteps - 4 * c);
+					const uint32_t fb = full0 + 8 * s, st = su32(sm + s * stage);
+					asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+					             :: "r"(fb), "r"(steps * STEP_A + bchunk) : "memory");
+					for (int j = 0; j < steps; j++) {
+						tma_load_4d(st + j * STEP_A, &xmap, c16 * 16, x0 + tap % 3 - 1, y0 + (tap / 3) % 3 - 1,
+						            z0 + tap / 9 - 1, fb);
+						if (++c16 == p.cg) { c16 = 0; tap++; }
+					}
+					asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+					             :: "r"(st + 4 * STEP_A), "l"(p.bk + (size_t)c * bchunk), "r"(bchunk), "r"(fb)
+					             : "memory");
+					issued = q + 1;
+				}
+			}
+		}
+		__syncwarp();
+	} else if (warp == 1) {
+		if (lane == 0) {
+			uint32_t q = 0, i = 0;
+			bool stop = false;
+			for (int tile = blockIdx.x; tile < p.tiles && !stop; tile += gridDim.x, i++) {
+				const uint32_t a = i & 1, ua = i >> 1;
+				if (ua > 0 && !wait_role(aempty0 + 8 * a, (ua - 1) & 1, abort_flag)) break;
+				tc_fence_after();
+				const uint32_t acc_t = tmem + a * (uint32_t)p.np;
+				for (int c = 0; c < p.nch; c++, q++) {
+					const int s = (int)(q % TS);
+					if (!wait_role(full0 + 8 * s, (q / TS) & 1, abort_flag)) { stop = true; break; }
+					tc_fence_after();
+					const int steps = min(4, p.ksteps - 4 * c);
+					const uint32_t a0 = su32(sm + s * stage), b0 = a0 + 4 * STEP_A;
+					for (int j = 0; j < steps; j++) {
+						const uint32_t acc = (c | j) != 0;
+						asm volatile("{\n\t.reg .pred q;\n\t"
+						             "setp.ne.b32 q, %4, 0;\n\t"
+						             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, q;\n\t}"
+						             :: "r"(acc_t), "l"(sw32(a0 + j * STEP_A)), "l"(sw32(b0 + j * bstep)), "r"(p.idesc),
+						                "r"(acc)
+						             : "memory");
+					}
+					asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+					             :: "r"(empty0 + 8 * s) : "memory");
+					mma_chunks = (int64_t)q + 1;
+				}
+				if (stop) break;
+				asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+				             :: "r"(afull0 + 8 * a) : "memory");
+			}
+		}
+		__syncwarp();
+	} else {
+		const int quarter = warp & 3;
+		uint32_t i = 0;
+		for (int tile = blockIdx.x; tile < p.tiles; tile += gridDim.x, i++) {
+			const uint32_t a = i & 1, ua = i >> 1;
+			int ok = 1;
+			if (lane == 0) ok = wait_role(afull0 + 8 * a, ua & 1, abort_flag);
+			if (!__shfl_sync(0xffffffffu, ok, 0)) break;
+			tc_fence_after();
+			const int64_t v = (int64_t)tile * TCM + quarter * 32 + lane;
+			const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + a * (uint32_t)p.np;
+			for (int c0 = 0; c0 < p.np; c0 += 16) {
+				float acc[16];
+				ld16(ta + (uint32_t)c0, acc);
+				#pragma unroll
+				for (int j = 0; j < 16; j++) {
+					const int co = c0 + j;
+					if (co >= p.cout) break;
+					float val = acc[j] + (p.bias ? __ldg(p.bias + co) : 0.0f);
+					if (p.relu) val = fmaxf(val, 0.0f);
+					const int64_t o = (int64_t)co * p.V + v;
+					if (p.residual) val += get((const TO *)p.residual, o);
+					put((TO *)p.out, o, val);
+				}
+			}
+			tc_fence_before();
+			__syncwarp();
+			if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(aempty0 + 8 * a) : "memory");
+		}
+	}
+	__syncthreads();
+	if (*abort_flag) {
+		/* bounded drain of the loads and tensor operations still in flight */
+		if (tid == 0)
+			for (uint32_t q = issued > (uint32_t)TS ? issued - TS : 0u; q < issued; q++)
+				bar_wait(full0 + 8 * (q % TS), (q / TS) & 1);
+		if (tid == 32 && mma_chunks > 0) {
+			const uint32_t q = (uint32_t)(mma_chunks - 1);
+			bar_wait(empty0 + 8 * (q % TS), (q / TS) & 1);
+		}
+	}
+	tc_fence_before();
+	__syncthreads();
+	tc_fence_after();
+	if (warp == 1)
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(tcols) : "memory");
+}
+
 std::mutex g_bk_lock;
 uint16_t *g_bk = nullptr;
 size_t g_bk_bytes = 0;
+uint8_t *g_cl = nullptr;
+size_t g_cl_bytes = 0;
+
+/* grows *buf to at least `bytes` (cudaFree synchronises: no earlier launch still reads it) */
+cudaError_t grow(uint8_t **buf, size_t *have, size_t bytes)
+{
+	if (bytes <= *have) return cudaSuccess;
+	cudaFree(*buf);
+	*buf = nullptr;
+	*have = 0;
+	const cudaError_t e = cudaMalloc((void **)buf, bytes);
+	if (e == cudaSuccess) *have = bytes;
+	return e;
+}
+
+/* rows of the volume tile by 128 voxels, so every 128-voxel tile is one TMA box */
+bool tma_geometry(const int32_t dims[3])
+{
+	const int W = dims[0], H = dims[1];
+	if (W <= 0 || H <= 0 || dims[2] <= 0) return false;
+	if (W <= TCM) return TCM % W == 0 && H % (TCM / W) == 0;
+	return W % TCM == 0;
+}
+
+bool conv3d_tma_launch(const void *in, int in_type, int cin, const uint16_t *w, const float *bias, const void *residual, void *out,
+                       int out_type, int cout, const int32_t dims[3], int relu, cudaStream_t s, cudaError_t &err)
+{
+	const auto enc = (PFN_cuTensorMapEncodeTiled_v12000)tensor_map_encoder();
+	if (!enc) return false;
+	const int cg = (cin + 15) / 16, np = (cout + 15) / 16 * 16;
+	if (np > 128 || cg > 32) return false;
+	const int ksteps = 27 * cg, nch = (ksteps + 3) / 4;
+	const int64_t V = (int64_t)dims[0] * dims[1] * dims[2];
+	ConvTma p{};
+	std::lock_guard<std::mutex> hold(g_bk_lock);
+	if ((err = grow((uint8_t **)&g_bk, &g_bk_bytes, (size_t)nch * 4 * np * 32)) != cudaSuccess) return true;
+	if ((err = grow(&g_cl, &g_cl_bytes, (size_t)V * cg * 32)) != cudaSuccess) return true;
+	CUtensorMap xmap;
+	const cuuint64_t gdim[4] = {(cuuint64_t)cg * 16, (cuuint64_t)dims[0], (cuuint64_t)dims[1], (cuuint64_t)dims[2]};
+	const cuuint64_t gstr[3] = {(cuuint64_t)cg * 32, (cuuint64_t)cg * 32 * dims[0],
+	                            (cuuint64_t)cg * 32 * dims[0] * dims[1]};
+	const cuuint32_t box[4] = {16, (cuuint32_t)std::min(dims[0], TCM), (cuuint32_t)std::max(1, TCM / dims[0]), 1};
+	const cuuint32_t estr[4] = {1, 1, 1, 1};
+	if (enc(&xmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, g_cl, gdim, gstr, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+	        CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
+	    CUDA_SUCCESS)
+		return false;
+	const int64_t wtotal = (int64_t)nch * 4 * np * 16;
+	prepare_weights_tma<<<(int)std::min<int64_t>((wtotal + 255) / 256, 1024), 256, 0, s>>>(
+	    (const __nv_bfloat16 *)w, g_bk, cin, cg, cout, np, nch * 4);
+	g_kernel_launches++;
+	if ((err = cudaGetLastError()) != cudaSuccess) return true;
+	const dim3 cgrid((unsigned)std::min<int64_t>((V + 255) / 256, (int64_t)device_sm_count() * 16), (unsigned)cg);
+	if (in_type == BF_UNET_F32) to_channels_last<<<cgrid, 256, 0, s>>>((const float *)in, (uint4 *)g_cl, cin, cg, V);
+	else                        to_channels_last<<<cgrid, 256, 0, s>>>((const uint16_t *)in, (uint4 *)g_cl, cin, cg, V);
+	g_kernel_launches++;
+	if ((err = cudaGetLastError()) != cudaSuccess) return true;
+	p.bk = (const uint8_t *)g_bk;
+	p.bias = bias;
+	p.residual = residual;
+	p.out = out;
+	p.cout = cout;
+	p.np = np;
+	p.cg = cg;
+	p.ksteps = ksteps;
+	p.nch = nch;
+	p.W = dims[0];
+	p.H = dims[1];
+	p.V = V;
+	p.relu = relu;
+	p.tiles = (int)(V / TCM);
+	p.idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(np >> 3) << 17) | ((uint32_t)(TCM >> 4) << 24);
+	const size_t smem = 1024 + (size_t)TS * (4 * STEP_A + 4 * np * 32) + (2 * TS + 4) * 8;
+	const void *fn = out_type == BF_UNET_F32 ? (const void *)conv3d_tma<float> : (const void *)conv3d_tma<__nv_bfloat16>;
+	if ((err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+		return true;
+	int occ = 1;
+	if ((err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, 192, smem)) != cudaSuccess) return true;
+	/* every resident CTA holds its tensor-memory columns for its whole life */
+	const int tcols = 2 * np <= 32 ? 32 : 2 * np <= 64 ? 64 : 2 * np <= 128 ? 128 : 256;
+	occ = std::max(1, std::min(occ, 512 / tcols));
+	const int grid = (int)std::min<int64_t>(p.tiles, (int64_t)device_sm_count() * occ);
+	if (out_type == BF_UNET_F32) conv3d_tma<float><<<grid, 192, smem, s>>>(xmap, p);
+	else                         conv3d_tma<__nv_bfloat16><<<grid, 192, smem, s>>>(xmap, p);
+	g_kernel_launches++;
+	err = cudaGetLastError();
+	return true;
+}
 
 } /* namespace */
 
-/* true when the tensor-core form was launched (BF16 input); false to fall back */
-bool conv3d_tc_launch(const void *in, int cin, const uint16_t *w, const float *bias, const void *residual, void *out,
+/* true when a tensor-core form was launched (err: its launch status); false to
+ * fall back to the direct kernel. BF16 inputs run on either form, FP32 inputs
+ * (rounded to BF16) on the TMA form only. */
+bool conv3d_tc_launch(const void *in, int in_type, int cin, const uint16_t *w, const float *bias, const void *residual, void *out,
                       int out_type, int cout, const int32_t dims[3], int relu, cudaStream_t s, cudaError_t &err)
 {
 	const char *env = std::getenv("OGL_BF_UNET_SIMT");
 	if (env && env[0] == '1') return false;
+	/* OGL_BF_UNET_TC=gather keeps the gathering form for every volume */
+	const char *form = std::getenv("OGL_BF_UNET_TC");
+	const bool gather_only = form && std::strcmp(form, "gather") == 0;
+	if (!gather_only && tma_geometry(dims) &&
+	    conv3d_tma_launch(in, in_type, cin, w, bias, residual, out, out_type, cout, dims, relu, s, err))
+		return true;
+	if (in_type != BF_UNET_BF16) return false;
 	const int cin_p = (cin + 7) / 8 * 8, np = (cout + 15) / 16 * 16;
 	if (np > 128 || cin_p > 512) return false;
 	const int nch = (27 * cin_p + TCK - 1) / TCK;
 	const size_t bk_bytes = (size_t)nch * np * 128;
 	ConvTc p{};
-	{
-		std::lock_guard<std::mutex> hold(g_bk_lock);
-		if (bk_bytes > g_bk_bytes) {
-			cudaFree(g_bk);                      /* synchronises: no earlier launch still reads it */
-			g_bk = nullptr;
-			g_bk_bytes = 0;
-			if ((err = cudaMalloc(&g_bk, bk_bytes)) != cudaSuccess) return true;
-			g_bk_bytes = bk_bytes;
-		}
-		p.bk = (const uint8_t *)g_bk;
-	}
+	std::lock_guard<std::mutex> hold(g_bk_lock);
+	if ((err = grow((uint8_t **)&g_bk, &g_bk_bytes, bk_bytes)) != cudaSuccess) return true;
+	p.bk = (const uint8_t *)g_bk;
 	const int64_t total = (int64_t)nch * np * TCK;
 	prepare_weights_tc<<<(int)std::min<int64_t>((total + 255) / 256, 1024), 256, 0, s>>>(
 	    (const __nv_bfloat16 *)w, g_bk, cin, cin_p, cout, np, nch);

@@ -102,6 +102,7 @@ def _bind(lib):
         "bf_unet_mse": [vp, vp, vp, vp, i64, vp],
         "bf_unet_adam": [vp, vp, vp, vp, vp, i64, f32, f32, f32, f32, i32, vp],
         "bf_unet_convert": [vp, i32, vp, i32, i64, f32, vp],
+        "bf_unet_ema": [vp, vp, vp, i64, f32, vp],
         "bf_synth_traces": [vp, vp, i32, vp, i32, i32, i32, f32, f32, f32, f32, f32, vp],
         "bf_unet_tc_errors": [vp],
     }
@@ -173,6 +174,9 @@ class Kernels:
         self._ok(self.lib.bf_unet_adam(self._p(w), self._p(g), self._p(m), self._p(v), self._p(w16), w.numel(), lr, b1,
                                        b2, eps, step, self.stream), "adam")
 
+    def ema(self, e, w, e16, decay):
+        self._ok(self.lib.bf_unet_ema(self._p(e), self._p(w), self._p(e16), w.numel(), decay, self.stream), "ema")
+
     def convert(self, x, y, scale=1.0):
         tx = BF16 if x.dtype == torch.bfloat16 else F32
         ty = BF16 if y.dtype == torch.bfloat16 else F32
@@ -200,10 +204,43 @@ class UNet:
                      b16=torch.empty(cout, dtype=torch.bfloat16, device=self.device))
             self.k.convert(L["w"], L["w16"])
             self.p[name] = L
+        self._reset_average()
         self.scratch = torch.empty(max(L["cin"] * L["cout"] * 27 for L in self.p.values()), dtype=torch.bfloat16,
                                    device=self.device)
         self.step = 0
         self.acts = None
+
+    def _reset_average(self):
+        """the moving average of the weights restarts from the current weights"""
+        for L in self.p.values():
+            L["we"], L["be"] = L["w"].clone(), L["b"].clone()
+            L["w16e"] = L["w16"].clone()
+
+    def average(self, decay):
+        """one step of the exponential moving average of the weights (bf_unet_ema)"""
+        for L in self.p.values():
+            self.k.ema(L["we"], L["w"], L["w16e"], decay)
+            self.k.ema(L["be"], L["b"], None, decay)
+
+    def _swap_average(self):
+        for L in self.p.values():
+            L["w16"], L["w16e"] = L["w16e"], L["w16"]
+            L["b"], L["be"] = L["be"], L["b"]
+            L["w"], L["we"] = L["we"], L["w"]
+
+    def averaged(self):
+        """context in which forward() (and state()) use the averaged weights"""
+        net = self
+
+        class _Ctx:
+            def __enter__(self):
+                net._swap_average()
+                return net
+
+            def __exit__(self, *exc):
+                net._swap_average()
+                return False
+        return _Ctx()
 
     def state(self):
         return {n: (L["w"].clone(), L["b"].clone()) for n, L in self.p.items()}
@@ -213,6 +250,7 @@ class UNet:
             self.p[n]["w"].copy_(torch.as_tensor(w))
             self.p[n]["b"].copy_(torch.as_tensor(b))
             self.k.convert(self.p[n]["w"], self.p[n]["w16"])
+        self._reset_average()
 
     def save_file(self, path):
         save_weights(path, self.state())
@@ -442,11 +480,27 @@ def make_dataset(n, seed0, points=(128, 128, 256), max_speckle=30000, kernels=No
     return X, Y, pm.dims
 
 
-def train(X, Y, steps, crop=(64, 64, 64), lr=1e-3, seed=0, log_every=100, net=None, kernels=None):
-    """Adam on random crops (one per step) of the pairs; returns the network and
-    the logged losses."""
+def lr_schedule(s, steps, lr, warmup=None, floor=0.05):
+    """learning rate of step s: linear warm-up over the first `warmup` steps
+    (steps / 20 by default), then a cosine decay from lr to floor * lr"""
+    warmup = max(1, steps // 20) if warmup is None else max(1, warmup)
+    ramp = min(1.0, (s + 1) / warmup)
+    t = min(1.0, max(0.0, (s - warmup) / max(1, steps - warmup)))
+    return lr * ramp * (floor + (1.0 - floor) * 0.5 * (1.0 + math.cos(math.pi * t)))
+
+
+def train(X, Y, steps, crop=(64, 64, 64), lr=1e-3, seed=0, log_every=100, net=None, kernels=None, ema=0.998,
+          eval_fn=None, eval_every=0):
+    """Adam on random crops (one per step) of the pairs, the learning rate from
+    lr_schedule, and an exponential moving average of the weights (decay `ema`,
+    ramped in as min(ema, (1 + s) / (10 + s))); returns the network, whose
+    averaged weights are the ones to evaluate (UNet.averaged), the logged losses
+    (mean training loss over each logging window) and, when eval_fn is given,
+    the curve [(step, eval_fn(net))] with the averaged weights every
+    `eval_every` steps and after the last."""
     k = kernels or Kernels()
     net = net or UNet(seed=seed, kernels=k)
+    curve = []
     rng = np.random.default_rng(seed)
     n, _, D, H, W = X.shape
     cx, cy, cz = crop
@@ -454,7 +508,7 @@ def train(X, Y, steps, crop=(64, 64, 64), lr=1e-3, seed=0, log_every=100, net=No
     x32 = torch.empty((2, cz, cy, cx), dtype=torch.float32, device="cuda")
     t32 = torch.empty_like(x32)
     gy = torch.empty_like(x32)
-    losses = []
+    losses, window = [], 0
     for s in range(steps):
         i = int(rng.integers(n))
         z0 = int(rng.integers(0, (D - cz) // 4 + 1)) * 4
@@ -464,12 +518,21 @@ def train(X, Y, steps, crop=(64, 64, 64), lr=1e-3, seed=0, log_every=100, net=No
         k.convert(xc, x32)
         k.convert(Y[i, :, z0:z0 + cz, y0:y0 + cy, x0:x0 + cx].contiguous(), t32)
         y = net.forward(xc, x32, crop)
-        loss.zero_()
-        k.mse(y, t32, gy, loss)
+        k.mse(y, t32, gy, loss)             # accumulates over the logging window
+        window += 1
         net.backward(gy)
-        net.adam(lr)
+        net.adam(lr_schedule(s, steps, lr))
+        net.average(min(ema, (1.0 + s) / (10.0 + s)))
         if log_every and (s % log_every == 0 or s == steps - 1):
-            losses.append((s, float(loss.item())))
+            losses.append((s, float(loss.item()) / window))
+            loss.zero_()
+            window = 0
+        if eval_fn is not None and ((eval_every and (s + 1) % eval_every == 0) or s == steps - 1):
+            if not curve or curve[-1][0] != s + 1:
+                with net.averaged():
+                    curve.append((s + 1, eval_fn(net)))
+    if eval_fn is not None:
+        return net, losses, curve
     return net, losses
 
 
