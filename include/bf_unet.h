@@ -38,10 +38,9 @@ uint32_t bf_unet_conv3d(const void *in, int32_t in_type, int32_t cin, const uint
 uint32_t bf_unet_tc_errors(void *stream);
 
 /* grad_in[ci] = sum_co w[co][ci] (flipped) * grad_out[co]; w_scratch holds
- * cin * cout * 27 bf16 (the transposed, flipped weights). On volumes whose rows
- * tile by 128 voxels (W a divisor of 128 and H a multiple of 128 / W, or W a
- * multiple of 128) grad_out is rounded to BF16 and the sum runs on the tensor
- * cores with FP32 accumulation; otherwise FP32 products on the direct kernel. */
+ * cin * cout * 27 bf16 (the transposed, flipped weights). grad_out is rounded to
+ * BF16 and the sum runs on the tensor cores with FP32 accumulation (the direct
+ * kernel with FP32 products where the tensor-core form does not apply). */
 uint32_t bf_unet_conv3d_grad_input(const float *grad_out, int32_t cout, const uint16_t *w, float *grad_in, int32_t cin,
                                    const int32_t dims[3], uint16_t *w_scratch, void *stream);
 

@@ -409,7 +409,7 @@ __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map
 /* 192 threads: warp 0 loads, warp 1 issues the MMAs (and owns tensor memory),
  * warps 2-5 run the epilogue (warp w reads accumulator lanes 32 (w % 4) ...). */
 template <typename TO>
-__global__ void __launch_bounds__(192)
+__global__ void __launch_bounds__(192, 1)
 conv3d_tma(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ ConvTma p)
 {
 	extern __shared__ uint8_t smem_raw[];
@@ -556,6 +556,248 @@ conv3d_tma(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ Con
 		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(tcols) : "memory");
 }
 
+/* ------------------------------ slab form ------------------------------ */
+
+constexpr int SLAB_ROWS = TCM + 2;               /* 128 positions and the x halo */
+constexpr int SLAB_PLANE = SLAB_ROWS * 16;       /* one 8-channel plane of a slab: 2080 B */
+constexpr int SLAB_MAX_STAGES = 8;
+constexpr int SLAB_BARS = 256;                   /* barrier area ahead of the stages */
+
+struct ConvSlab {
+	const uint8_t *planes;   /* [G][PR][8] bf16: zero-padded channels-last planes */
+	const uint8_t *bk;       /* [9 (dz, dy)][3 dx][G][np][8] bf16 */
+	const float   *bias;
+	const void    *residual;
+	void          *out;
+	int64_t        PR;       /* rows (positions) per plane */
+	int64_t        V;
+	int32_t        G, np, cout, stages, stage_bytes, a_bytes, b_bytes;
+	int32_t        W, H, D, Wp, Hp;
+	int32_t        P0, tiles;
+	int32_t        relu;
+	uint32_t       idesc;
+};
+
+/* K-major operand without swizzling: core matrices of 8 rows x 16 B (rows 16 B
+ * apart); SBO between core matrices along M (N), LBO between them along K;
+ * descriptor version 1 */
+__device__ __forceinline__ uint64_t interleaved(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+	uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+	d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+	d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+	d |= (uint64_t)1 << 46;
+	return d;
+}
+
+/* channels-first [cin][V] (BF16, or FP32 rounded to BF16) -> planes [G][PR][8]:
+ * plane g holds channels 8 g ... 8 g + 7 of every position P of the volume
+ * padded by one zero voxel on each face ((D + 2) x (H + 2) x (W + 2), x
+ * fastest), positions beyond it zero. Thread per (position, plane): 8 coalesced
+ * loads, one 16-byte store (a warp stores 512 contiguous bytes). */
+template <typename TI>
+__global__ void __launch_bounds__(256)
+to_padded_planes(const TI *__restrict__ in, uint4 *__restrict__ planes, int cin, int W, int H, int D, int64_t PR)
+{
+	const int g = blockIdx.y;
+	const int Wp = W + 2;
+	const int64_t hw = (int64_t)(H + 2) * Wp, V = (int64_t)W * H * D;
+	for (int64_t P = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; P < PR; P += (int64_t)gridDim.x * blockDim.x) {
+		const int64_t zp = P / hw, rem = P - zp * hw;
+		const int yp = (int)(rem / Wp), xp = (int)(rem - (int64_t)yp * Wp);
+		uint32_t w[4] = {0u, 0u, 0u, 0u};
+		if (zp >= 1 && zp <= D && yp >= 1 && yp <= H && xp >= 1 && xp <= W) {
+			const int64_t v = ((zp - 1) * H + (yp - 1)) * (int64_t)W + (xp - 1);
+			#pragma unroll
+			for (int k = 0; k < 8; k += 2) {
+				const int c0 = g * 8 + k;
+				const uint32_t lo = c0 < cin ? bf16_bits(in, (int64_t)c0 * V + v) : 0u;
+				const uint32_t hi = c0 + 1 < cin ? bf16_bits(in, (int64_t)(c0 + 1) * V + v) : 0u;
+				w[k >> 1] = lo | (hi << 16);
+			}
+		}
+		planes[(int64_t)g * PR + P] = make_uint4(w[0], w[1], w[2], w[3]);
+	}
+}
+
+/* weights [9 (dz, dy)][3 dx][G][np][8]: element (n, channel 8 g + c) of tap
+ * (dz, dy, dx); zero beyond cout and cin */
+__global__ void __launch_bounds__(256)
+prepare_weights_slab(const __nv_bfloat16 *__restrict__ w, uint16_t *__restrict__ bk, int cin, int G, int cout, int np)
+{
+	const int64_t total = (int64_t)27 * G * np * 8;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+		const int c = (int)(i & 7);
+		int64_t r = i >> 3;
+		const int n = (int)(r % np);
+		r /= np;
+		const int g = (int)(r % G);
+		const int tap = (int)(r / G);          /* (dz, dy) * 3 + dx = the tap index */
+		const int ci = g * 8 + c;
+		uint16_t v = 0;
+		if (n < cout && ci < cin) v = __bfloat16_as_ushort(w[((int64_t)n * cin + ci) * 27 + tap]);
+		bk[i] = v;
+	}
+}
+
+/* 192 threads: warp 0 loads, warp 1 issues the MMAs (and owns tensor memory),
+ * warps 2-5 run the epilogue. One stage is one (dz, dy) slab of a tile: per
+ * 8-channel plane the 130 consecutive padded positions from the tile's first
+ * position + (dz, dy) offset - 1 (one bulk copy each), and the weights of the
+ * three dx taps; the dx taps are the same rows read from offsets 0, 16 and 32 B. */
+template <typename TO>
+__global__ void __launch_bounds__(192, 1)
+conv3d_slab(const __grid_constant__ ConvSlab p)
+{
+	extern __shared__ uint8_t smem_raw[];
+	uint8_t *sm = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+	uint64_t *bars = (uint64_t *)sm;          /* full[8], empty[8], acc_full[2], acc_empty[2] */
+	uint8_t *stages = sm + SLAB_BARS;
+	__shared__ uint32_t tmem_slot;
+	__shared__ int abort_word;
+	volatile int *abort_flag = &abort_word;
+
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const int S = p.stages;
+	const uint32_t full0 = su32(bars), empty0 = full0 + 8 * SLAB_MAX_STAGES, afull0 = empty0 + 8 * SLAB_MAX_STAGES,
+	               aempty0 = afull0 + 16;
+	const uint32_t tcols = 2 * p.np <= 32 ? 32u : 2 * p.np <= 64 ? 64u : 2 * p.np <= 128 ? 128u : 256u;
+	if (warp == 1) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+		             :: "r"(su32(&tmem_slot)), "r"(tcols) : "memory");
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+	}
+	if (tid == 0) {
+		for (int i = 0; i < 2 * SLAB_MAX_STAGES + 2; i++)
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(full0 + 8 * i), "r"(1) : "memory");
+		for (int i = 0; i < 2; i++)
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(aempty0 + 8 * i), "r"(4) : "memory");
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+		abort_word = 0;
+	}
+	tc_fence_before();
+	__syncthreads();
+	tc_fence_after();
+	const uint32_t tmem = tmem_slot;
+	const int64_t hw = (int64_t)p.Hp * p.Wp;
+	uint32_t issued = 0;
+	int64_t mma_chunks = 0;
+
+	if (warp == 0) {
+		if (lane == 0) {
+			uint32_t q = 0;
+			for (int tile = blockIdx.x; tile < p.tiles && !*abort_flag; tile += gridDim.x) {
+				const int64_t first = (int64_t)p.P0 + (int64_t)tile * TCM - 1;
+				for (int sl = 0; sl < 9; sl++, q++) {
+					const int s = (int)(q % S);
+					const uint32_t u = q / S;
+					if (u > 0 && !wait_role(empty0 + 8 * s, (u - 1) & 1, abort_flag)) break;
+					if (*abort_flag) break;
+					const int64_t start = first + ((int64_t)(sl / 3 - 1) * p.Hp + (sl % 3 - 1)) * p.Wp;
+					const uint32_t fb = full0 + 8 * s, st = su32(stages + (size_t)s * p.stage_bytes);
+					asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+					             :: "r"(fb), "r"(p.a_bytes + p.b_bytes) : "memory");
+					for (int g = 0; g < p.G; g++)
+						asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+						             :: "r"(st + g * SLAB_PLANE), "l"(p.planes + ((int64_t)g * p.PR + start) * 16),
+						                "r"(SLAB_PLANE), "r"(fb)
+						             : "memory");
+					asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+					             :: "r"(st + p.a_bytes), "l"(p.bk + (size_t)sl * p.b_bytes), "r"(p.b_bytes), "r"(fb)
+					             : "memory");
+					issued = q + 1;
+				}
+			}
+		}
+		__syncwarp();
+	} else if (warp == 1) {
+		if (lane == 0) {
+			uint32_t q = 0, i = 0;
+			bool stop = false;
+			const uint32_t bplane = (uint32_t)p.np * 16;
+			for (int tile = blockIdx.x; tile < p.tiles && !stop; tile += gridDim.x, i++) {
+				const uint32_t a = i & 1, ua = i >> 1;
+				if (ua > 0 && !wait_role(aempty0 + 8 * a, (ua - 1) & 1, abort_flag)) break;
+				tc_fence_after();
+				const uint32_t acc_t = tmem + a * (uint32_t)p.np;
+				for (int sl = 0; sl < 9; sl++, q++) {
+					const int s = (int)(q % S);
+					if (!wait_role(full0 + 8 * s, (q / S) & 1, abort_flag)) { stop = true; break; }
+					tc_fence_after();
+					const uint32_t a0 = su32(stages + (size_t)s * p.stage_bytes), b0 = a0 + (uint32_t)p.a_bytes;
+					for (int dx = 0; dx < 3; dx++)
+						for (int j = 0; j < p.G; j += 2) {
+							const uint32_t acc = (sl | dx | j) != 0;
+							const uint64_t da = interleaved(a0 + j * SLAB_PLANE + dx * 16, SLAB_PLANE, 128);
+							const uint64_t db = interleaved(b0 + (uint32_t)(dx * p.G + j) * bplane, bplane, 128);
+							asm volatile("{\n\t.reg .pred q;\n\t"
+							             "setp.ne.b32 q, %4, 0;\n\t"
+							             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, q;\n\t}"
+							             :: "r"(acc_t), "l"(da), "l"(db), "r"(p.idesc), "r"(acc) : "memory");
+						}
+					asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+					             :: "r"(empty0 + 8 * s) : "memory");
+					mma_chunks = (int64_t)q + 1;
+				}
+				if (stop) break;
+				asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+				             :: "r"(afull0 + 8 * a) : "memory");
+			}
+		}
+		__syncwarp();
+	} else {
+		const int quarter = warp & 3;
+		uint32_t i = 0;
+		for (int tile = blockIdx.x; tile < p.tiles; tile += gridDim.x, i++) {
+			const uint32_t a = i & 1, ua = i >> 1;
+			int ok = 1;
+			if (lane == 0) ok = wait_role(afull0 + 8 * a, ua & 1, abort_flag);
+			if (!__shfl_sync(0xffffffffu, ok, 0)) break;
+			tc_fence_after();
+			const int64_t P = (int64_t)p.P0 + (int64_t)tile * TCM + quarter * 32 + lane;
+			const int64_t zp = P / hw, rem = P - zp * hw;
+			const int yp = (int)(rem / p.Wp), xp = (int)(rem - (int64_t)yp * p.Wp);
+			const bool inside = zp >= 1 && zp <= p.D && yp >= 1 && yp <= p.H && xp >= 1 && xp <= p.W;
+			const int64_t v = ((zp - 1) * p.H + (yp - 1)) * (int64_t)p.W + (xp - 1);
+			const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + a * (uint32_t)p.np;
+			for (int c0 = 0; c0 < p.np; c0 += 16) {
+				float acc[16];
+				ld16(ta + (uint32_t)c0, acc);
+				if (inside) {
+					#pragma unroll
+					for (int j = 0; j < 16; j++) {
+						const int co = c0 + j;
+						if (co >= p.cout) break;
+						float val = acc[j] + (p.bias ? __ldg(p.bias + co) : 0.0f);
+						if (p.relu) val = fmaxf(val, 0.0f);
+						const int64_t o = (int64_t)co * p.V + v;
+						if (p.residual) val += get((const TO *)p.residual, o);
+						put((TO *)p.out, o, val);
+					}
+				}
+			}
+			tc_fence_before();
+			__syncwarp();
+			if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(aempty0 + 8 * a) : "memory");
+		}
+	}
+	__syncthreads();
+	if (*abort_flag) {
+		if (tid == 0)
+			for (uint32_t q = issued > (uint32_t)S ? issued - S : 0u; q < issued; q++)
+				bar_wait(full0 + 8 * (q % S), (q / S) & 1);
+		if (tid == 32 && mma_chunks > 0) {
+			const uint32_t q = (uint32_t)(mma_chunks - 1);
+			bar_wait(empty0 + 8 * (q % S), (q / S) & 1);
+		}
+	}
+	tc_fence_before();
+	__syncthreads();
+	tc_fence_after();
+	if (warp == 1)
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(tcols) : "memory");
+}
+
 std::mutex g_bk_lock;
 uint16_t *g_bk = nullptr;
 size_t g_bk_bytes = 0;
@@ -581,6 +823,20 @@ bool tma_geometry(const int32_t dims[3])
 	if (W <= 0 || H <= 0 || dims[2] <= 0) return false;
 	if (W <= TCM) return TCM % W == 0 && H % (TCM / W) == 0;
 	return W % TCM == 0;
+}
+
+/* resident CTAs per SM for `smem` bytes of dynamic shared memory, 192 threads and
+ * `tcols` tensor-memory columns held for the CTA's whole life */
+cudaError_t resident_ctas(size_t smem, int tcols, int &occ)
+{
+	int dev = 0, sm_bytes = 0, reserved = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sm_bytes, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+	if (e == cudaSuccess) e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+	if (e != cudaSuccess) return e;
+	occ = sm_bytes / (int)(smem + (size_t)reserved + 64);
+	occ = std::max(1, std::min({occ, 2048 / 192, 512 / tcols}));
+	return cudaSuccess;
 }
 
 bool conv3d_tma_launch(const void *in, int in_type, int cin, const uint16_t *w, const float *bias, const void *residual, void *out,
@@ -635,14 +891,78 @@ bool conv3d_tma_launch(const void *in, int in_type, int cin, const uint16_t *w, 
 	const void *fn = out_type == BF_UNET_F32 ? (const void *)conv3d_tma<float> : (const void *)conv3d_tma<__nv_bfloat16>;
 	if ((err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
 		return true;
-	int occ = 1;
-	if ((err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, 192, smem)) != cudaSuccess) return true;
-	/* every resident CTA holds its tensor-memory columns for its whole life */
 	const int tcols = 2 * np <= 32 ? 32 : 2 * np <= 64 ? 64 : 2 * np <= 128 ? 128 : 256;
-	occ = std::max(1, std::min(occ, 512 / tcols));
+	int occ = 1;
+	if ((err = resident_ctas(smem, tcols, occ)) != cudaSuccess) return true;
 	const int grid = (int)std::min<int64_t>(p.tiles, (int64_t)device_sm_count() * occ);
 	if (out_type == BF_UNET_F32) conv3d_tma<float><<<grid, 192, smem, s>>>(xmap, p);
 	else                         conv3d_tma<__nv_bfloat16><<<grid, 192, smem, s>>>(xmap, p);
+	g_kernel_launches++;
+	err = cudaGetLastError();
+	return true;
+}
+
+bool conv3d_slab_launch(const void *in, int in_type, int cin, const uint16_t *w, const float *bias, const void *residual,
+                        void *out, int out_type, int cout, const int32_t dims[3], int relu, cudaStream_t s,
+                        cudaError_t &err)
+{
+	const int G = (cin + 15) / 16 * 2, np = (cout + 15) / 16 * 16;
+	if (np > 128) return false;
+	const int W = dims[0], H = dims[1], D = dims[2];
+	const int64_t Wp = W + 2, Hp = H + 2, Vp = (int64_t)(D + 2) * Hp * Wp;
+	const int64_t PR = Vp + 256;
+	if (PR > INT32_MAX) return false;
+	ConvSlab p{};
+	p.a_bytes = G * SLAB_PLANE;
+	p.b_bytes = 3 * G * np * 16;
+	p.stage_bytes = (p.a_bytes + p.b_bytes + 127) / 128 * 128;
+	if (p.stage_bytes > 100 * 1024) return false;
+	p.stages = std::max(2, std::min(SLAB_MAX_STAGES, 112 * 1024 / p.stage_bytes));
+	std::lock_guard<std::mutex> hold(g_bk_lock);
+	if ((err = grow((uint8_t **)&g_bk, &g_bk_bytes, (size_t)p.b_bytes * 9)) != cudaSuccess) return true;
+	if ((err = grow(&g_cl, &g_cl_bytes, (size_t)G * PR * 16)) != cudaSuccess) return true;
+	const int64_t wtotal = (int64_t)27 * G * np * 8;
+	prepare_weights_slab<<<(int)std::min<int64_t>((wtotal + 255) / 256, 1024), 256, 0, s>>>(
+	    (const __nv_bfloat16 *)w, g_bk, cin, G, cout, np);
+	g_kernel_launches++;
+	if ((err = cudaGetLastError()) != cudaSuccess) return true;
+	const dim3 cgrid((unsigned)std::min<int64_t>((PR + 255) / 256, (int64_t)device_sm_count() * 16), (unsigned)G);
+	if (in_type == BF_UNET_F32)
+		to_padded_planes<<<cgrid, 256, 0, s>>>((const float *)in, (uint4 *)g_cl, cin, W, H, D, PR);
+	else
+		to_padded_planes<<<cgrid, 256, 0, s>>>((const uint16_t *)in, (uint4 *)g_cl, cin, W, H, D, PR);
+	g_kernel_launches++;
+	if ((err = cudaGetLastError()) != cudaSuccess) return true;
+	p.planes = g_cl;
+	p.bk = (const uint8_t *)g_bk;
+	p.bias = bias;
+	p.residual = residual;
+	p.out = out;
+	p.PR = PR;
+	p.V = (int64_t)W * H * D;
+	p.G = G;
+	p.np = np;
+	p.cout = cout;
+	p.W = W;
+	p.H = H;
+	p.D = D;
+	p.Wp = (int32_t)Wp;
+	p.Hp = (int32_t)Hp;
+	p.P0 = (int32_t)((Hp + 1) * Wp + 1);
+	const int64_t P1 = ((int64_t)D * Hp + H) * Wp + W;
+	p.tiles = (int32_t)((P1 - p.P0 + TCM) / TCM);
+	p.relu = relu;
+	p.idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(np >> 3) << 17) | ((uint32_t)(TCM >> 4) << 24);
+	const size_t smem = 1024 + SLAB_BARS + (size_t)p.stages * p.stage_bytes;
+	const void *fn = out_type == BF_UNET_F32 ? (const void *)conv3d_slab<float> : (const void *)conv3d_slab<__nv_bfloat16>;
+	if ((err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+		return true;
+	const int tcols = 2 * np <= 32 ? 32 : 2 * np <= 64 ? 64 : 2 * np <= 128 ? 128 : 256;
+	int occ = 1;
+	if ((err = resident_ctas(smem, tcols, occ)) != cudaSuccess) return true;
+	const int grid = (int)std::min<int64_t>(p.tiles, (int64_t)device_sm_count() * occ);
+	if (out_type == BF_UNET_F32) conv3d_slab<float><<<grid, 192, smem, s>>>(p);
+	else                         conv3d_slab<__nv_bfloat16><<<grid, 192, smem, s>>>(p);
 	g_kernel_launches++;
 	err = cudaGetLastError();
 	return true;
@@ -658,10 +978,15 @@ bool conv3d_tc_launch(const void *in, int in_type, int cin, const uint16_t *w, c
 {
 	const char *env = std::getenv("OGL_BF_UNET_SIMT");
 	if (env && env[0] == '1') return false;
-	/* OGL_BF_UNET_TC=gather keeps the gathering form for every volume */
+	/* OGL_BF_UNET_TC selects a form: slab (the default), tma (volumes whose rows
+	 * tile by 128 voxels) or gather (BF16 inputs) */
 	const char *form = std::getenv("OGL_BF_UNET_TC");
 	const bool gather_only = form && std::strcmp(form, "gather") == 0;
-	if (!gather_only && tma_geometry(dims) &&
+	const bool tma = form && std::strcmp(form, "tma") == 0;
+	if (!gather_only && !tma &&
+	    conv3d_slab_launch(in, in_type, cin, w, bias, residual, out, out_type, cout, dims, relu, s, err))
+		return true;
+	if (tma && tma_geometry(dims) &&
 	    conv3d_tma_launch(in, in_type, cin, w, bias, residual, out, out_type, cout, dims, relu, s, err))
 		return true;
 	if (in_type != BF_UNET_BF16) return false;
