@@ -78,6 +78,7 @@ def parse():
                          "channel DAS + U-Net against full-aperture DAS")
     ap.add_argument("--train-pairs", type=int, default=2000)
     ap.add_argument("--train-steps", type=int, default=4000)
+    ap.add_argument("--train-lr", type=float, default=5e-4, help="peak learning rate of the learned variant")
     return ap.parse_args()
 
 
@@ -743,8 +744,8 @@ def run_learned(args, peaks):
     Xt, Yt, _ = Lm.make_dataset(16, 900000, kernels=k)
     t0 = time.perf_counter()
     held_out = lambda n: float(np.mean(Lm.evaluate(n, Xt, Yt, dims, kernels=k)[1]))
-    net, losses, curve = Lm.train(X, Y, args.train_steps, crop=(64, 64, 64), lr=1e-3, log_every=250, kernels=k,
-                                  eval_fn=held_out, eval_every=max(1, args.train_steps // 8))
+    net, losses, curve = Lm.train(X, Y, args.train_steps, crop=(64, 64, 64), lr=args.train_lr, log_every=250,
+                                  kernels=k, eval_fn=held_out, eval_every=max(1, args.train_steps // 8))
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     del X, Y
@@ -829,7 +830,8 @@ def run_learned(args, peaks):
         "training": {"data_s": t_data, "train_s": t_train, "loss": losses,
                      "held_out_mean_nrmse_db": curve,
                      "held_out_monotone": all(b[1] <= a[1] for a, b in zip(curve, curve[1:])),
-                     "schedule": "warm-up steps/20, cosine 1e-3 -> 5e-5; weights averaged (decay 0.998)"}}))
+                     "schedule": f"warm-up steps/10, cosine {args.train_lr:g} -> {0.05 * args.train_lr:g}; "
+                                 "weights averaged (decay 0.998)"}}))
     return 0
 
 

@@ -63,12 +63,12 @@ template <int TY, int SEGB> __host__ __device__ constexpr int stg_rc()
 }
 
 /* dynamic shared memory of a block: two buffers of stg_rc windows, their first
- * segments, two mbarriers, the box, the block's transmit interval per receive
- * channel (receive channels < 256) */
+ * segments, four mbarriers (full and empty per buffer), the stop word, the box,
+ * the block's transmit interval per receive channel (receive channels < 256) */
 template <int INTERP, int TY, bool H> __host__ __device__ constexpr int stg_smem_bytes()
 {
 	return 2 * stg_rc<TY, stg_seg_bytes<INTERP, H>()>() * stg_wm<TY>() * stg_seg_bytes<INTERP, H>() +
-	       2 * stg_rc<TY, stg_seg_bytes<INTERP, H>()>() * 4 + 2 * 8 + 8 * 4 + 2 * 256 * 4;
+	       2 * stg_rc<TY, stg_seg_bytes<INTERP, H>()>() * 4 + 5 * 8 + 8 * 4 + 2 * 256 * 4;
 }
 
 __device__ __forceinline__ uint32_t stg_smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -84,6 +84,27 @@ __device__ __forceinline__ bool stg_wait(uint32_t bar, uint32_t parity, long lon
 		             : "=r"(done) : "r"(bar), "r"(parity) : "memory");
 		if (done) return true;
 		if (clock64() - t0 > limit) return false;
+	}
+}
+
+/* stg_wait that also gives up when the block's stop word is set; a wait that runs
+ * out sets the stop word and the error word */
+__device__ __forceinline__ bool stg_wait_or_stop(uint32_t bar, uint32_t parity, volatile int *stop, unsigned *error)
+{
+	const long long t0 = clock64();
+	while (true) {
+		uint32_t done;
+		asm volatile("{\n\t.reg .pred p;\n\t"
+		             "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+		             "selp.u32 %0, 1, 0, p;\n\t}"
+		             : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+		if (done) return true;
+		if (*stop) return false;
+		if (clock64() - t0 > STG_WAIT_CYCLES) {
+			*stop = 1;
+			atomicExch(error, 1u);
+			return false;
+		}
 	}
 }
 
@@ -386,18 +407,23 @@ __device__ __forceinline__ void hercules_staged_body(const DasParams &p, const f
 	constexpr int BUFB = RC * WM * SEGB;
 	uint8_t *bufs = smem;
 	int *win_lo = (int *)(smem + 2 * BUFB);
-	uint64_t *bars = (uint64_t *)(win_lo + 2 * RC);
-	float *boxs = (float *)(bars + 2);
+	uint64_t *bars = (uint64_t *)(win_lo + 2 * RC);        /* full[2], empty[2] */
+	volatile int *stop = (volatile int *)(bars + 4);
+	float *boxs = (float *)(bars + 5);
 	int *tb_lo = (int *)(boxs + 8), *tb_hi = tb_lo + 256;
-	const int tid = threadIdx.x;
+	const int tid = threadIdx.x, lane = tid & 31;
 	constexpr unsigned FULL = 0xffffffffu;
+	constexpr int WARPS = 128 / 32;
 
 	for (int i = tid; i < 2 * BUFB / 16; i += blockDim.x) ((uint4 *)bufs)[i] = make_uint4(0u, 0u, 0u, 0u);
 	for (int i = tid; i < 256; i += blockDim.x) { tb_lo[i] = p.T; tb_hi[i] = -1; }
 	if (tid == 0) {
 		asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(stg_smem_u32(bars)), "r"(RC) : "memory");
 		asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(stg_smem_u32(bars + 1)), "r"(RC) : "memory");
+		asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(stg_smem_u32(bars + 2)), "r"(WARPS) : "memory");
+		asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(stg_smem_u32(bars + 3)), "r"(WARPS) : "memory");
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+		*stop = 0;
 		boxs[0] = box_in.qc[0]; boxs[1] = box_in.qc[1]; boxs[2] = box_in.qc[2];
 		boxs[3] = box_in.rq; boxs[4] = box_in.dtx_lo; boxs[5] = box_in.dtx_hi;
 	}
@@ -466,7 +492,12 @@ __device__ __forceinline__ void hercules_staged_body(const DasParams &p, const f
 	if (cr >= u_end) return;
 	int ct0 = tb_lo[cr];
 	issue(cr, ct0, 0);
-	uint32_t phase = 0;
+	/* Chunk c sits in buffer c % 2. Its copies complete full[c % 2]; every warp
+	 * arrives on empty[c % 2] when it has summed the chunk, and the copies of
+	 * chunk c + 2 wait for that, so a warp can run a chunk ahead of the slowest
+	 * instead of meeting it at a block barrier after every chunk. */
+	uint32_t c = 0;
+	int last_issued = 0;                /* the last chunk this thread's copies went to (chunk 0 above) */
 	int buf = 0, prev_r = -1;
 	int w_lo = 0, w_hi = -1;
 	float f2 = 0.0f;
@@ -480,7 +511,13 @@ __device__ __forceinline__ void hercules_staged_body(const DasParams &p, const f
 			nt0 = nr < u_end ? tb_lo[nr] : 0;
 		}
 		const bool has_next = nr < u_end;
-		if (has_next) issue(nr, nt0, buf ^ 1);
+		if (has_next && tid < RC) {
+			/* buffer buf ^ 1 last held chunk c - 1: wait until every warp summed it */
+			if (c == 0 || stg_wait_or_stop(stg_smem_u32(bars + 2 + (buf ^ 1)), ((c - 1) >> 1) & 1u, stop, p.wait_error)) {
+				issue(nr, nt0, buf ^ 1);
+				last_issued = (int)c + 1;
+			}
+		}
 		if (cr != prev_r) {
 			prev_r = cr;
 			f2 = fixed2(cr);
@@ -490,20 +527,8 @@ __device__ __forceinline__ void hercules_staged_body(const DasParams &p, const f
 			w_lo = __reduce_min_sync(FULL, lo);
 			w_hi = __reduce_max_sync(FULL, hi);
 		}
-		const bool got = stg_wait(stg_smem_u32(bars + buf), (phase >> buf) & 1u);
-		phase ^= 1u << buf;
-		if (__syncthreads_or(!got)) {
-			/* a copy did not arrive in time: report, drain what this block issued, stop */
-			if (tid == 0) {
-				atomicExch(p.wait_error, 1u);
-				stg_wait(stg_smem_u32(bars + buf), ((phase >> buf) & 1u) ^ 1u);
-				if (has_next) stg_wait(stg_smem_u32(bars + (buf ^ 1)), (phase >> (buf ^ 1)) & 1u);
-			}
-			__syncthreads();
-			#pragma unroll
-			for (int k = 0; k < NV; k++) sx[k] = sy[k] = __int_as_float(0x7fc00000);
-			return;
-		}
+		int ok = stg_wait_or_stop(stg_smem_u32(bars + buf), (c >> 1) & 1u, stop, p.wait_error) && !*stop;
+		if (!__shfl_sync(FULL, ok, 0)) break;
 		const int last = min(ct0 + RC - 1, tb_hi[cr]);
 		int t = max(ct0, w_lo);
 		const int te = min(last, w_hi);
@@ -561,11 +586,24 @@ __device__ __forceinline__ void hercules_staged_body(const DasParams &p, const f
 			#pragma unroll
 			for (int k = 0; k < NV; k++) { sx[k] += ax[k]; sy[k] += ay[k]; ax[k] = ay[k] = 0.0f; }
 		}
-		__syncthreads();
+		__syncwarp();
+		if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(stg_smem_u32(bars + 2 + buf)) : "memory");
 		if (!has_next) break;
 		cr = nr;
 		ct0 = nt0;
 		buf ^= 1;
+		c++;
+	}
+	/* every warp is out of its loop (each wait is bounded), so the stop word is final */
+	__syncthreads();
+	if (*stop) {
+		/* a wait ran out in this block: the copy threads drain what they issued
+		 * (bounded), every voxel of the block reports NaN */
+		if (tid < RC)
+			for (int k = max(0, last_issued - 1); k <= last_issued; k++)   /* chunk k sits in buffer k % 2 */
+				stg_wait(stg_smem_u32(bars + (k & 1)), ((uint32_t)k >> 1) & 1u);
+		#pragma unroll
+		for (int k = 0; k < NV; k++) sx[k] = sy[k] = __int_as_float(0x7fc00000);
 	}
 }
 

@@ -482,22 +482,25 @@ def make_dataset(n, seed0, points=(128, 128, 256), max_speckle=30000, kernels=No
 
 def lr_schedule(s, steps, lr, warmup=None, floor=0.05):
     """learning rate of step s: linear warm-up over the first `warmup` steps
-    (steps / 20 by default), then a cosine decay from lr to floor * lr"""
-    warmup = max(1, steps // 20) if warmup is None else max(1, warmup)
+    (steps / 10 by default), then a cosine decay from lr to floor * lr"""
+    warmup = max(1, steps // 10) if warmup is None else max(1, warmup)
     ramp = min(1.0, (s + 1) / warmup)
     t = min(1.0, max(0.0, (s - warmup) / max(1, steps - warmup)))
     return lr * ramp * (floor + (1.0 - floor) * 0.5 * (1.0 + math.cos(math.pi * t)))
 
 
-def train(X, Y, steps, crop=(64, 64, 64), lr=1e-3, seed=0, log_every=100, net=None, kernels=None, ema=0.998,
-          eval_fn=None, eval_every=0):
+def train(X, Y, steps, crop=(64, 64, 64), lr=5e-4, seed=0, log_every=100, net=None, kernels=None, ema=0.998,
+          eval_fn=None, eval_every=0, normalize=True):
     """Adam on random crops (one per step) of the pairs, the learning rate from
     lr_schedule, and an exponential moving average of the weights (decay `ema`,
-    ramped in as min(ema, (1 + s) / (10 + s))); returns the network, whose
-    averaged weights are the ones to evaluate (UNet.averaged), the logged losses
-    (mean training loss over each logging window) and, when eval_fn is given,
-    the curve [(step, eval_fn(net))] with the averaged weights every
-    `eval_every` steps and after the last."""
+    ramped in as min(ema, (1 + s) / (10 + s))). With `normalize` each crop's
+    loss is its squared error divided by its target's mean square (its NRMSE
+    squared, the quantity evaluate reports per volume), so that crops of bright
+    speckle do not outweigh dark ones. Returns the network, whose averaged
+    weights are the ones to evaluate (UNet.averaged), the logged losses (mean
+    training loss over each logging window) and, when eval_fn is given, the
+    curve [(step, eval_fn(net))] with the averaged weights every `eval_every`
+    steps and after the last."""
     k = kernels or Kernels()
     net = net or UNet(seed=seed, kernels=k)
     curve = []
@@ -508,7 +511,10 @@ def train(X, Y, steps, crop=(64, 64, 64), lr=1e-3, seed=0, log_every=100, net=No
     x32 = torch.empty((2, cz, cy, cx), dtype=torch.float32, device="cuda")
     t32 = torch.empty_like(x32)
     gy = torch.empty_like(x32)
-    losses, window = [], 0
+    zero = torch.zeros_like(x32)
+    scratch = torch.empty_like(x32)
+    stats = torch.zeros(2, dtype=torch.float32, device="cuda")     # target mean square, loss
+    losses, window, acc = [], 0, 0.0
     for s in range(steps):
         i = int(rng.integers(n))
         z0 = int(rng.integers(0, (D - cz) // 4 + 1)) * 4
@@ -518,15 +524,24 @@ def train(X, Y, steps, crop=(64, 64, 64), lr=1e-3, seed=0, log_every=100, net=No
         k.convert(xc, x32)
         k.convert(Y[i, :, z0:z0 + cz, y0:y0 + cy, x0:x0 + cx].contiguous(), t32)
         y = net.forward(xc, x32, crop)
-        k.mse(y, t32, gy, loss)             # accumulates over the logging window
+        if normalize:
+            stats.zero_()
+            k.mse(t32, zero, scratch, stats[0:1])
+            k.mse(y, t32, gy, stats[1:2])
+            energy, mse = (float(v) for v in stats.cpu())
+            inv = 1.0 / max(energy, 1e-12)
+            k.convert(gy, gy, inv)
+            acc += mse * inv
+        else:
+            k.mse(y, t32, gy, loss)         # accumulates over the logging window
         window += 1
         net.backward(gy)
         net.adam(lr_schedule(s, steps, lr))
         net.average(min(ema, (1.0 + s) / (10.0 + s)))
         if log_every and (s % log_every == 0 or s == steps - 1):
-            losses.append((s, float(loss.item()) / window))
+            losses.append((s, (acc if normalize else float(loss.item())) / window))
             loss.zero_()
-            window = 0
+            window, acc = 0, 0.0
         if eval_fn is not None and ((eval_every and (s + 1) % eval_every == 0) or s == steps - 1):
             if not curve or curve[-1][0] != s + 1:
                 with net.averaged():
@@ -550,3 +565,80 @@ def evaluate(net, X, Y, dims, kernels=None):
         base.append(nrmse_db(x32, t32))
         learned.append(nrmse_db(y, t32))
     return np.array(base), np.array(learned)
+
+
+def time_layers(layers, reps=5, forms=("",), seed=0):
+    """Mean CUDA-event milliseconds of BF16 convolution layers [(cin, cout, (W, H, D))]
+    with random inputs and weights, for each OGL_BF_UNET_TC form in `forms`
+    ("" = the default form; "simt" = the direct kernel)."""
+    import os
+    k = Kernels()
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    res = {}
+    for cin, cout, dims in layers:
+        W, H, D = dims
+        x = torch.randn((cin, D, H, W), device="cuda", generator=g).to(torch.bfloat16)
+        w = (torch.randn(cout * cin * 27, device="cuda", generator=g) * 0.05).to(torch.bfloat16)
+        b = torch.zeros(cout, device="cuda")
+        out = torch.empty((cout, D, H, W), device="cuda", dtype=torch.bfloat16)
+        for form in forms:
+            saved = {v: os.environ.get(v) for v in ("OGL_BF_UNET_TC", "OGL_BF_UNET_SIMT")}
+            os.environ["OGL_BF_UNET_SIMT"] = "1" if form == "simt" else "0"
+            os.environ["OGL_BF_UNET_TC"] = "" if form == "simt" else form
+            try:
+                k.conv(x, cin, w, b, out, cout, dims, True)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(reps):
+                    k.conv(x, cin, w, b, out, cout, dims, True)
+                e1.record()
+                torch.cuda.synchronize()
+            finally:
+                for v, val in saved.items():
+                    if val is None:
+                        os.environ.pop(v, None)
+                    else:
+                        os.environ[v] = val
+            res[f"{cin}->{cout} {W}x{H}x{D} {form or 'default'}"] = e0.elapsed_time(e1) / reps
+    if k.lib.bf_unet_tc_errors(k.stream):
+        raise RuntimeError("a tensor-core convolution's bounded wait ran out")
+    return res
+
+
+def _main(argv=None):
+    """python -m ogl_beamforming_cuda_gb300.learned conv CIN COUT W H D [--reps N] [--forms a,b]:
+    times one BF16 convolution layer; python -m ... forward W H D [--reps N]: times the
+    whole network's forward pass (random weights). Prints one JSON line."""
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(prog="python -m ogl_beamforming_cuda_gb300.learned")
+    ap.add_argument("what", choices=["conv", "forward"])
+    ap.add_argument("sizes", type=int, nargs="+")
+    ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--forms", default="")
+    a = ap.parse_args(argv)
+    torch.cuda.set_device(0)
+    if a.what == "conv":
+        cin, cout, W, H, D = a.sizes
+        print(json.dumps(time_layers([(cin, cout, (W, H, D))], a.reps, tuple(a.forms.split(",")))))
+        return 0
+    W, H, D = a.sizes
+    net = UNet()
+    x32 = torch.randn((2, D, H, W), device="cuda")
+    x16 = x32.to(torch.bfloat16)
+    net.forward(x16, x32, (W, H, D))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(a.reps):
+        net.forward(x16, x32, (W, H, D))
+    e1.record()
+    torch.cuda.synchronize()
+    print(json.dumps({"unet_forward_ms": e0.elapsed_time(e1) / a.reps, "dims": [W, H, D],
+                      "tc_errors": int(net.k.lib.bf_unet_tc_errors(net.k.stream))}))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(_main())
