@@ -831,7 +831,7 @@ def run_learned(args, peaks):
                      "held_out_mean_nrmse_db": curve,
                      "held_out_monotone": all(b[1] <= a[1] for a, b in zip(curve, curve[1:])),
                      "schedule": f"warm-up steps/10, cosine {args.train_lr:g} -> {0.05 * args.train_lr:g}; "
-                                 "weights averaged (decay 0.998)"}}))
+                                 "weights averaged from the initial network (decay 0.999)"}}))
     return 0
 
 

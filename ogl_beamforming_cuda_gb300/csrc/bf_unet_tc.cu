@@ -572,6 +572,7 @@ struct ConvSlab {
 	int64_t        PR;       /* rows (positions) per plane */
 	int64_t        V;
 	int32_t        G, np, cout, stages, stage_bytes, a_bytes, b_bytes;
+	int32_t        resident;  /* all 27 taps' weights (9 b_bytes) stay in shared memory, copied once */
 	int32_t        W, H, D, Wp, Hp;
 	int32_t        P0, tiles;
 	int32_t        relu;
@@ -651,8 +652,9 @@ conv3d_slab(const __grid_constant__ ConvSlab p)
 {
 	extern __shared__ uint8_t smem_raw[];
 	uint8_t *sm = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-	uint64_t *bars = (uint64_t *)sm;          /* full[8], empty[8], acc_full[2], acc_empty[2] */
-	uint8_t *stages = sm + SLAB_BARS;
+	uint64_t *bars = (uint64_t *)sm;          /* full[8], empty[8], acc_full[2], acc_empty[2], weights */
+	uint8_t *wres = sm + SLAB_BARS;                         /* resident weights (p.resident) */
+	uint8_t *stages = wres + (p.resident ? 9 * p.b_bytes : 0);
 	__shared__ uint32_t tmem_slot;
 	__shared__ int abort_word;
 	volatile int *abort_flag = &abort_word;
@@ -660,7 +662,7 @@ conv3d_slab(const __grid_constant__ ConvSlab p)
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const int S = p.stages;
 	const uint32_t full0 = su32(bars), empty0 = full0 + 8 * SLAB_MAX_STAGES, afull0 = empty0 + 8 * SLAB_MAX_STAGES,
-	               aempty0 = afull0 + 16;
+	               aempty0 = afull0 + 16, wbar = aempty0 + 16;
 	const uint32_t tcols = 2 * p.np <= 32 ? 32u : 2 * p.np <= 64 ? 64u : 2 * p.np <= 128 ? 128u : 256u;
 	if (warp == 1) {
 		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
@@ -672,6 +674,7 @@ conv3d_slab(const __grid_constant__ ConvSlab p)
 			asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(full0 + 8 * i), "r"(1) : "memory");
 		for (int i = 0; i < 2; i++)
 			asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(aempty0 + 8 * i), "r"(4) : "memory");
+		asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(wbar), "r"(1) : "memory");
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 		abort_word = 0;
 	}
@@ -680,6 +683,12 @@ conv3d_slab(const __grid_constant__ ConvSlab p)
 	tc_fence_after();
 	const uint32_t tmem = tmem_slot;
 	const int64_t hw = (int64_t)p.Hp * p.Wp;
+	if (tid == 0 && p.resident) {
+		const uint32_t wb = (uint32_t)(9 * p.b_bytes);
+		asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(wbar), "r"(wb) : "memory");
+		asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+		             :: "r"(su32(wres)), "l"(p.bk), "r"(wb), "r"(wbar) : "memory");
+	}
 	uint32_t issued = 0;
 	int64_t mma_chunks = 0;
 
@@ -696,15 +705,16 @@ conv3d_slab(const __grid_constant__ ConvSlab p)
 					const int64_t start = first + ((int64_t)(sl / 3 - 1) * p.Hp + (sl % 3 - 1)) * p.Wp;
 					const uint32_t fb = full0 + 8 * s, st = su32(stages + (size_t)s * p.stage_bytes);
 					asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
-					             :: "r"(fb), "r"(p.a_bytes + p.b_bytes) : "memory");
+					             :: "r"(fb), "r"(p.a_bytes + (p.resident ? 0 : p.b_bytes)) : "memory");
 					for (int g = 0; g < p.G; g++)
 						asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
 						             :: "r"(st + g * SLAB_PLANE), "l"(p.planes + ((int64_t)g * p.PR + start) * 16),
 						                "r"(SLAB_PLANE), "r"(fb)
 						             : "memory");
-					asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-					             :: "r"(st + p.a_bytes), "l"(p.bk + (size_t)sl * p.b_bytes), "r"(p.b_bytes), "r"(fb)
-					             : "memory");
+					if (!p.resident)
+						asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+						             :: "r"(st + p.a_bytes), "l"(p.bk + (size_t)sl * p.b_bytes), "r"(p.b_bytes), "r"(fb)
+						             : "memory");
 					issued = q + 1;
 				}
 			}
@@ -715,6 +725,7 @@ conv3d_slab(const __grid_constant__ ConvSlab p)
 			uint32_t q = 0, i = 0;
 			bool stop = false;
 			const uint32_t bplane = (uint32_t)p.np * 16;
+			if (p.resident && !wait_role(wbar, 0, abort_flag)) stop = true;
 			for (int tile = blockIdx.x; tile < p.tiles && !stop; tile += gridDim.x, i++) {
 				const uint32_t a = i & 1, ua = i >> 1;
 				if (ua > 0 && !wait_role(aempty0 + 8 * a, (ua - 1) & 1, abort_flag)) break;
@@ -724,7 +735,8 @@ conv3d_slab(const __grid_constant__ ConvSlab p)
 					const int s = (int)(q % S);
 					if (!wait_role(full0 + 8 * s, (q / S) & 1, abort_flag)) { stop = true; break; }
 					tc_fence_after();
-					const uint32_t a0 = su32(stages + (size_t)s * p.stage_bytes), b0 = a0 + (uint32_t)p.a_bytes;
+					const uint32_t a0 = su32(stages + (size_t)s * p.stage_bytes);
+					const uint32_t b0 = p.resident ? su32(wres) + (uint32_t)(sl * p.b_bytes) : a0 + (uint32_t)p.a_bytes;
 					for (int dx = 0; dx < 3; dx++)
 						for (int j = 0; j < p.G; j += 2) {
 							const uint32_t acc = (sl | dx | j) != 0;
@@ -783,9 +795,11 @@ conv3d_slab(const __grid_constant__ ConvSlab p)
 	}
 	__syncthreads();
 	if (*abort_flag) {
-		if (tid == 0)
+		if (tid == 0) {
+			if (p.resident) bar_wait(wbar, 0);
 			for (uint32_t q = issued > (uint32_t)S ? issued - S : 0u; q < issued; q++)
 				bar_wait(full0 + 8 * (q % S), (q / S) & 1);
+		}
 		if (tid == 32 && mma_chunks > 0) {
 			const uint32_t q = (uint32_t)(mma_chunks - 1);
 			bar_wait(empty0 + 8 * (q % S), (q / S) & 1);
@@ -915,9 +929,13 @@ bool conv3d_slab_launch(const void *in, int in_type, int cin, const uint16_t *w,
 	ConvSlab p{};
 	p.a_bytes = G * SLAB_PLANE;
 	p.b_bytes = 3 * G * np * 16;
-	p.stage_bytes = (p.a_bytes + p.b_bytes + 127) / 128 * 128;
+	/* the weights stay resident when they take at most 48 KB (the full-resolution
+	 * layers); otherwise each stage carries its slab's three taps */
+	p.resident = 9 * p.b_bytes <= 48 * 1024;
+	p.stage_bytes = (p.a_bytes + (p.resident ? 0 : p.b_bytes) + 127) / 128 * 128;
 	if (p.stage_bytes > 100 * 1024) return false;
-	p.stages = std::max(2, std::min(SLAB_MAX_STAGES, 112 * 1024 / p.stage_bytes));
+	const int wres_bytes = p.resident ? 9 * p.b_bytes : 0;
+	p.stages = std::max(2, std::min(SLAB_MAX_STAGES, (112 * 1024 - wres_bytes) / p.stage_bytes));
 	std::lock_guard<std::mutex> hold(g_bk_lock);
 	if ((err = grow((uint8_t **)&g_bk, &g_bk_bytes, (size_t)p.b_bytes * 9)) != cudaSuccess) return true;
 	if ((err = grow(&g_cl, &g_cl_bytes, (size_t)G * PR * 16)) != cudaSuccess) return true;
@@ -953,7 +971,7 @@ bool conv3d_slab_launch(const void *in, int in_type, int cin, const uint16_t *w,
 	p.tiles = (int32_t)((P1 - p.P0 + TCM) / TCM);
 	p.relu = relu;
 	p.idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(np >> 3) << 17) | ((uint32_t)(TCM >> 4) << 24);
-	const size_t smem = 1024 + SLAB_BARS + (size_t)p.stages * p.stage_bytes;
+	const size_t smem = 1024 + SLAB_BARS + (size_t)wres_bytes + (size_t)p.stages * p.stage_bytes;
 	const void *fn = out_type == BF_UNET_F32 ? (const void *)conv3d_slab<float> : (const void *)conv3d_slab<__nv_bfloat16>;
 	if ((err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
 		return true;

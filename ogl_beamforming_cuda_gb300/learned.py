@@ -489,18 +489,17 @@ def lr_schedule(s, steps, lr, warmup=None, floor=0.05):
     return lr * ramp * (floor + (1.0 - floor) * 0.5 * (1.0 + math.cos(math.pi * t)))
 
 
-def train(X, Y, steps, crop=(64, 64, 64), lr=5e-4, seed=0, log_every=100, net=None, kernels=None, ema=0.998,
-          eval_fn=None, eval_every=0, normalize=True):
+def train(X, Y, steps, crop=(64, 64, 64), lr=5e-4, seed=0, log_every=100, net=None, kernels=None, ema=0.999,
+          eval_fn=None, eval_every=0):
     """Adam on random crops (one per step) of the pairs, the learning rate from
-    lr_schedule, and an exponential moving average of the weights (decay `ema`,
-    ramped in as min(ema, (1 + s) / (10 + s))). With `normalize` each crop's
-    loss is its squared error divided by its target's mean square (its NRMSE
-    squared, the quantity evaluate reports per volume), so that crops of bright
-    speckle do not outweigh dark ones. Returns the network, whose averaged
-    weights are the ones to evaluate (UNet.averaged), the logged losses (mean
-    training loss over each logging window) and, when eval_fn is given, the
-    curve [(step, eval_fn(net))] with the averaged weights every `eval_every`
-    steps and after the last."""
+    lr_schedule, and an exponential moving average of the weights (decay `ema`
+    from the first step: the average starts at the initial network, whose output
+    is close to its input, and moves to the trained weights over about
+    1 / (1 - ema) steps). Returns the network, whose averaged weights are the
+    ones to evaluate (UNet.averaged), the logged losses (mean training loss over
+    each logging window) and, when eval_fn is given, the curve
+    [(step, eval_fn(net))] with the averaged weights every `eval_every` steps and
+    after the last."""
     k = kernels or Kernels()
     net = net or UNet(seed=seed, kernels=k)
     curve = []
@@ -511,10 +510,7 @@ def train(X, Y, steps, crop=(64, 64, 64), lr=5e-4, seed=0, log_every=100, net=No
     x32 = torch.empty((2, cz, cy, cx), dtype=torch.float32, device="cuda")
     t32 = torch.empty_like(x32)
     gy = torch.empty_like(x32)
-    zero = torch.zeros_like(x32)
-    scratch = torch.empty_like(x32)
-    stats = torch.zeros(2, dtype=torch.float32, device="cuda")     # target mean square, loss
-    losses, window, acc = [], 0, 0.0
+    losses, window = [], 0
     for s in range(steps):
         i = int(rng.integers(n))
         z0 = int(rng.integers(0, (D - cz) // 4 + 1)) * 4
@@ -524,24 +520,15 @@ def train(X, Y, steps, crop=(64, 64, 64), lr=5e-4, seed=0, log_every=100, net=No
         k.convert(xc, x32)
         k.convert(Y[i, :, z0:z0 + cz, y0:y0 + cy, x0:x0 + cx].contiguous(), t32)
         y = net.forward(xc, x32, crop)
-        if normalize:
-            stats.zero_()
-            k.mse(t32, zero, scratch, stats[0:1])
-            k.mse(y, t32, gy, stats[1:2])
-            energy, mse = (float(v) for v in stats.cpu())
-            inv = 1.0 / max(energy, 1e-12)
-            k.convert(gy, gy, inv)
-            acc += mse * inv
-        else:
-            k.mse(y, t32, gy, loss)         # accumulates over the logging window
+        k.mse(y, t32, gy, loss)             # accumulates over the logging window
         window += 1
         net.backward(gy)
         net.adam(lr_schedule(s, steps, lr))
-        net.average(min(ema, (1.0 + s) / (10.0 + s)))
+        net.average(ema)
         if log_every and (s % log_every == 0 or s == steps - 1):
-            losses.append((s, (acc if normalize else float(loss.item())) / window))
+            losses.append((s, float(loss.item()) / window))
             loss.zero_()
-            window, acc = 0, 0.0
+            window = 0
         if eval_fn is not None and ((eval_every and (s + 1) % eval_every == 0) or s == steps - 1):
             if not curve or curve[-1][0] != s + 1:
                 with net.averaged():

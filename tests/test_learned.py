@@ -239,7 +239,7 @@ def test_training_improves_on_subsampled_das():
     # 1500 Adam steps (warm-up and cosine decay from 1e-3, averaged weights); the
     # float atomics of the weight gradient make each short training take its own path
     mean_db = lambda n: float(np.mean(Lm.evaluate(n, Xt, Yt, dims, kernels=k)[1]))
-    net, losses, curve = Lm.train(X, Y, 1500, crop=(32, 32, 32), lr=1e-3, log_every=100, kernels=k,
+    net, losses, curve = Lm.train(X, Y, 1500, crop=(32, 32, 32), lr=1e-3, log_every=100, kernels=k, ema=0.995,
                                   eval_fn=mean_db, eval_every=500)
     with net.averaged():
         base, learned = Lm.evaluate(net, Xt, Yt, dims, kernels=k)
