@@ -21,18 +21,22 @@
 #include "bf_das_math.cuh"
 #include "bf_das_generic.cuh"
 #include "bf_das_hercules.cuh"
+#include "bf_das_staged.cuh"
 #include "bf_das_forces.cuh"
 
 namespace bf {
 
 /* GENERAL = false: HERCULES tiles (up to 80 registers, 6 CTAs per SM), from the
- * FP32 table or, with H (DAS precision 1), the FP16 table; true: tiles of the
- * general path (FORCES), compiled on their own (64 registers, 8 CTAs per SM)
- * with their parameters copied to registers per tile. */
+ * FP32 table (staged in shared memory, as das_hercules_staged, for acquisitions
+ * marked `staged`; dynamic shared memory stg_smem_bytes) or, with H (DAS
+ * precision 1), the FP16 table; true: tiles of the general path (FORCES),
+ * compiled on their own (64 registers, 8 CTAs per SM) with their parameters
+ * copied to registers per tile. */
 template <int INTERP, bool GENERAL, bool H = false>
 __global__ void __launch_bounds__(DAS_THREADS, GENERAL ? 8 : 6)
 das_batch(const __grid_constant__ DasBatchArgs args, const int4 *__restrict__ items, int n_items, int *next)
 {
+	extern __shared__ __align__(128) uint8_t batch_smem[];
 	__shared__ int sitem;
 	while (true) {
 		__syncthreads();                        /* every thread has read the previous item */
@@ -43,6 +47,15 @@ das_batch(const __grid_constant__ DasBatchArgs args, const int4 *__restrict__ it
 		const int4 w = __ldg(items + it);
 		const DasBatchAcq &a = args.acq[w.x];
 		if (!GENERAL) {
+			if constexpr (INTERP != INTERP_NEAREST && !H && DAS_THREADS == 128) {
+				if (a.staged) {
+					if (a.path == DAS_BATCH_HERC_VOLUME)
+						hercules_tile_staged<INTERP, 4, false>(a.p, a.table, w.y, w.z, w.w, 0, batch_smem);
+					else
+						hercules_tile_staged<INTERP, 1, false>(a.p, a.table, w.y, w.z, w.w, 0, batch_smem);
+					continue;
+				}
+			}
 			if (a.path == DAS_BATCH_HERC_VOLUME) hercules_tile<INTERP, 4, DAS_THREADS, H>(a.p, a.table, w.y, w.z, w.w, 0);
 			else                                 hercules_tile<INTERP, 1, DAS_THREADS, H>(a.p, a.table, w.y, w.z, w.w, 0);
 		} else {
@@ -90,9 +103,15 @@ cudaError_t launch_das_batch(const DasBatchArgs &args, const int4 *items, int n_
 		if (args.acq[i].p.frame && args.acq[i].p.rx_step < 1) return cudaErrorInvalidValue;
 	cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), s);
 	if (e != cudaSuccess) return e;
+	/* shared memory of the staged tiles (volume and plane tiles stage the same windows) */
+	const size_t stg = interp == INTERP_CUBIC ? stg_smem_bytes<INTERP_CUBIC, 4, false>()
+	                   : interp == INTERP_LINEAR ? stg_smem_bytes<INTERP_LINEAR, 4, false>() : 0;
+	static_assert(stg_smem_bytes<INTERP_CUBIC, 4, false>() == stg_smem_bytes<INTERP_CUBIC, 1, false>() &&
+	              stg_smem_bytes<INTERP_LINEAR, 4, false>() == stg_smem_bytes<INTERP_LINEAR, 1, false>(),
+	              "volume and plane tiles share one shared-memory size");
 #define BF_BATCH(I) (general ? das_batch<I, true><<<ctas, DAS_THREADS, 0, s>>>(args, items, n_items, counter) \
                      : half  ? das_batch<I, false, true><<<ctas, DAS_THREADS, 0, s>>>(args, items, n_items, counter) \
-                             : das_batch<I, false><<<ctas, DAS_THREADS, 0, s>>>(args, items, n_items, counter))
+                             : das_batch<I, false><<<ctas, DAS_THREADS, stg, s>>>(args, items, n_items, counter))
 	switch (interp) {
 	case INTERP_CUBIC:  BF_BATCH(INTERP_CUBIC); break;
 	case INTERP_LINEAR: BF_BATCH(INTERP_LINEAR); break;

@@ -191,6 +191,11 @@ static bool use_staged(const DasParams &p)
 	return p.wait_error != nullptr && p.T <= 256 && p.loop_end <= 256 && (p.rot_table != 0 || !(p.fc > 0.0f));
 }
 
+bool das_hercules_use_staged(const DasParams &p)
+{
+	return !p.half_table && use_staged(p);
+}
+
 template <int INTERP, int TY, bool H>
 static int staged_occupancy()
 {

@@ -156,6 +156,9 @@ bool        das_hercules_supported(const DasParams &p);
 /* blocks of one channel group of the HERCULES launch, and resident blocks per SM */
 int64_t     das_hercules_tiles(const DasParams &p);
 int         das_hercules_blocks_per_sm(const DasParams &p);
+/* the HERCULES fast path of p reads its FP32 table staged in shared memory
+ * (blocks whose windows do not fit still run the unstaged tile code) */
+bool        das_hercules_use_staged(const DasParams &p);
 int64_t     das_hercules_table_bytes(const DasParams &p);
 cudaError_t launch_das_hercules(const DasParams &p, float4 *table, cudaStream_t s);
 /* FORCES fast path (bf_das_forces.cu): the same per-frame table (das_hercules_table_bytes
@@ -173,7 +176,7 @@ struct DasBatchAcq {
 	DasParams     p;
 	const float4 *table;       /* HERCULES interpolation table (das_hercules_table_bytes) */
 	int32_t       path;        /* DasBatchPath */
-	int32_t       reserved;
+	int32_t       staged;      /* HERCULES tiles read the FP32 table staged in shared memory */
 };
 /* up to DAS_BATCH_MAX acquisitions per launch, passed by value in the kernel's
  * parameter space (read through the constant cache, like a single launch's) */

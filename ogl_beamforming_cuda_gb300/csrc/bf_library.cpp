@@ -1194,6 +1194,10 @@ bool batch_items(bool volume_tiles)
 			d.p = a.das;
 			d.table = a.das_table;
 			d.path = a.path;
+			d.staged = a.path != DAS_BATCH_GENERIC && das_hercules_use_staged(a.das) ? 1 : 0;
+			/* OGL_BF_DAS_STAGED=require (tests): a staged tile that cannot stage writes NaN */
+			const char *stg_env = std::getenv("OGL_BF_DAS_STAGED");
+			d.p.stage_only = d.staged && stg_env && std::strcmp(stg_env, "require") == 0;
 			const double vox = a.path == DAS_BATCH_HERC_VOLUME ? 256.0 : 128.0;
 			order.push_back({vox * a.das.T * a.das.C, k});
 		}

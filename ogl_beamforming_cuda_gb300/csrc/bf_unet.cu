@@ -222,84 +222,92 @@ __global__ void relu_grad_k(float *__restrict__ g, const __nv_bfloat16 *__restri
 		if (!(__bfloat162float(a[i]) > 0.0f)) g[i] = 0.0f;
 }
 
+/* The pooling and upsampling kernels walk rows: block b takes rows b, b + grid,
+ * ... of its output (row = (channel * depth + z) * height + y), a row's threads
+ * its x positions, so the index arithmetic runs once per row. */
 template <typename TI, typename TO>
 __global__ void avgpool2_k(const TI *__restrict__ in, TO *__restrict__ out, int c, int W, int H, int D)
 {
 	const int w2 = W / 2, h2 = H / 2, d2 = D / 2;
-	const int64_t n = (int64_t)c * d2 * h2 * w2;
-	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-		const int x = (int)(i % w2);
-		int64_t r = i / w2;
-		const int y = (int)(r % h2);
-		r /= h2;
-		const int z = (int)(r % d2);
-		const int64_t ch = r / d2;
-		const size_t base = (size_t)ch * D * H * W;
-		float s = 0.0f;
-		#pragma unroll
-		for (int dz = 0; dz < 2; dz++)
+	const int64_t rows = (int64_t)c * d2 * h2;
+	for (int64_t row = blockIdx.x; row < rows; row += gridDim.x) {
+		const int y = (int)(row % h2);
+		const int64_t cz = row / h2;
+		const int z = (int)(cz % d2);
+		const int64_t ch = cz / d2;
+		const size_t base = (((size_t)ch * D + 2 * z) * H + 2 * y) * W;
+		const size_t plane = (size_t)H * W;
+		for (int x = threadIdx.x; x < w2; x += blockDim.x) {
+			float s = 0.0f;
 			#pragma unroll
-			for (int dy = 0; dy < 2; dy++)
+			for (int dz = 0; dz < 2; dz++)
 				#pragma unroll
-				for (int dx = 0; dx < 2; dx++)
-					s += ld(in, base + ((size_t)(2 * z + dz) * H + 2 * y + dy) * W + 2 * x + dx);
-		st(out, i, 0.125f * s);
+				for (int dy = 0; dy < 2; dy++)
+					#pragma unroll
+					for (int dx = 0; dx < 2; dx++)
+						s += ld(in, base + dz * plane + (size_t)dy * W + 2 * x + dx);
+			st(out, row * w2 + x, 0.125f * s);
+		}
 	}
 }
 
 __global__ void avgpool2_grad_k(const float *__restrict__ go, float *__restrict__ gi, int c, int W, int H, int D,
                                 int accumulate)
 {
-	const int64_t n = (int64_t)c * D * H * W;
 	const int w2 = W / 2, h2 = H / 2, d2 = D / 2;
-	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-		const int x = (int)(i % W);
-		int64_t r = i / W;
-		const int y = (int)(r % H);
-		r /= H;
-		const int z = (int)(r % D);
-		const int64_t ch = r / D;
-		const float v = 0.125f * go[(((size_t)ch * d2 + z / 2) * h2 + y / 2) * w2 + x / 2];
-		gi[i] = accumulate ? gi[i] + v : v;
+	const int64_t rows = (int64_t)c * D * H;
+	for (int64_t row = blockIdx.x; row < rows; row += gridDim.x) {
+		const int y = (int)(row % H);
+		const int64_t cz = row / H;
+		const int z = (int)(cz % D);
+		const int64_t ch = cz / D;
+		const float *src = go + (((size_t)ch * d2 + z / 2) * h2 + y / 2) * w2;
+		float *dst = gi + row * W;
+		for (int x = threadIdx.x; x < W; x += blockDim.x) {
+			const float v = 0.125f * src[x / 2];
+			dst[x] = accumulate ? dst[x] + v : v;
+		}
 	}
 }
 
 template <typename TI, typename TO>
 __global__ void upsample2_k(const TI *__restrict__ in, TO *__restrict__ out, int c, int W, int H, int D)
 {
-	const int64_t n = (int64_t)c * D * H * W;
 	const int w2 = W / 2, h2 = H / 2, d2 = D / 2;
-	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-		const int x = (int)(i % W);
-		int64_t r = i / W;
-		const int y = (int)(r % H);
-		r /= H;
-		const int z = (int)(r % D);
-		const int64_t ch = r / D;
-		st(out, i, ld(in, (((size_t)ch * d2 + z / 2) * h2 + y / 2) * w2 + x / 2));
+	const int64_t rows = (int64_t)c * D * H;
+	for (int64_t row = blockIdx.x; row < rows; row += gridDim.x) {
+		const int y = (int)(row % H);
+		const int64_t cz = row / H;
+		const int z = (int)(cz % D);
+		const int64_t ch = cz / D;
+		const size_t src = (((size_t)ch * d2 + z / 2) * h2 + y / 2) * w2;
+		const size_t dst = (size_t)row * W;
+		for (int x = threadIdx.x; x < W; x += blockDim.x) st(out, dst + x, ld(in, src + x / 2));
 	}
 }
 
 __global__ void upsample2_grad_k(const float *__restrict__ go, float *__restrict__ gi, int c, int W, int H, int D)
 {
 	const int w2 = W / 2, h2 = H / 2, d2 = D / 2;
-	const int64_t n = (int64_t)c * d2 * h2 * w2;
-	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-		const int x = (int)(i % w2);
-		int64_t r = i / w2;
-		const int y = (int)(r % h2);
-		r /= h2;
-		const int z = (int)(r % d2);
-		const int64_t ch = r / d2;
-		const size_t base = (size_t)ch * D * H * W;
-		float s = 0.0f;
-		#pragma unroll
-		for (int dz = 0; dz < 2; dz++)
+	const int64_t rows = (int64_t)c * d2 * h2;
+	for (int64_t row = blockIdx.x; row < rows; row += gridDim.x) {
+		const int y = (int)(row % h2);
+		const int64_t cz = row / h2;
+		const int z = (int)(cz % d2);
+		const int64_t ch = cz / d2;
+		const size_t base = (((size_t)ch * D + 2 * z) * H + 2 * y) * W;
+		const size_t plane = (size_t)H * W;
+		for (int x = threadIdx.x; x < w2; x += blockDim.x) {
+			float s = 0.0f;
 			#pragma unroll
-			for (int dy = 0; dy < 2; dy++)
+			for (int dz = 0; dz < 2; dz++)
 				#pragma unroll
-				for (int dx = 0; dx < 2; dx++) s += go[base + ((size_t)(2 * z + dz) * H + 2 * y + dy) * W + 2 * x + dx];
-		gi[i] = s;
+				for (int dy = 0; dy < 2; dy++)
+					#pragma unroll
+					for (int dx = 0; dx < 2; dx++)
+						s += go[base + dz * plane + (size_t)dy * W + 2 * x + dx];
+			gi[row * w2 + x] = s;
+		}
 	}
 }
 
@@ -382,6 +390,8 @@ synth_k(const float *__restrict__ pos, const float *__restrict__ amp, int n_scat
 }
 
 int grid_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, (int64_t)device_sm_count() * 32); }
+/* blocks for a row walk over `rows` rows */
+int grid_rows(int64_t rows) { return (int)std::max<int64_t>(1, std::min<int64_t>(rows, (int64_t)device_sm_count() * 64)); }
 
 } /* namespace */
 } /* namespace bf */
@@ -485,15 +495,15 @@ uint32_t bf_unet_avgpool2(const void *in, int32_t in_type, void *out, int32_t ou
 	if (!in || !out || c <= 0 || !dims_in || dims_in[0] % 2 || dims_in[1] % 2 || dims_in[2] % 2) return 0;
 	cudaStream_t s = (cudaStream_t)stream;
 	const int W = dims_in[0], H = dims_in[1], D = dims_in[2];
-	const int64_t n = (int64_t)c * (D / 2) * (H / 2) * (W / 2);
+	const int g = grid_rows((int64_t)c * (D / 2) * (H / 2)), t = std::min(128, std::max(32, W / 2));
 	if (in_type == BF_UNET_BF16 && out_type == BF_UNET_BF16)
-		avgpool2_k<<<grid_for(n), 256, 0, s>>>((const __nv_bfloat16 *)in, (__nv_bfloat16 *)out, c, W, H, D);
+		avgpool2_k<<<g, t, 0, s>>>((const __nv_bfloat16 *)in, (__nv_bfloat16 *)out, c, W, H, D);
 	else if (in_type == BF_UNET_F32 && out_type == BF_UNET_F32)
-		avgpool2_k<<<grid_for(n), 256, 0, s>>>((const float *)in, (float *)out, c, W, H, D);
+		avgpool2_k<<<g, t, 0, s>>>((const float *)in, (float *)out, c, W, H, D);
 	else if (in_type == BF_UNET_BF16)
-		avgpool2_k<<<grid_for(n), 256, 0, s>>>((const __nv_bfloat16 *)in, (float *)out, c, W, H, D);
+		avgpool2_k<<<g, t, 0, s>>>((const __nv_bfloat16 *)in, (float *)out, c, W, H, D);
 	else
-		avgpool2_k<<<grid_for(n), 256, 0, s>>>((const float *)in, (__nv_bfloat16 *)out, c, W, H, D);
+		avgpool2_k<<<g, t, 0, s>>>((const float *)in, (__nv_bfloat16 *)out, c, W, H, D);
 	g_kernel_launches++;
 	return BF_OK(cudaGetLastError());
 }
@@ -502,8 +512,8 @@ uint32_t bf_unet_avgpool2_grad(const float *grad_out, float *grad_in, int32_t c,
                                int32_t accumulate, void *stream)
 {
 	if (!grad_out || !grad_in || c <= 0 || !dims_in) return 0;
-	const int64_t n = (int64_t)c * dims_in[0] * dims_in[1] * dims_in[2];
-	avgpool2_grad_k<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(grad_out, grad_in, c, dims_in[0], dims_in[1],
+	const int g = grid_rows((int64_t)c * dims_in[2] * dims_in[1]), t = std::min(128, std::max(32, dims_in[0]));
+	avgpool2_grad_k<<<g, t, 0, (cudaStream_t)stream>>>(grad_out, grad_in, c, dims_in[0], dims_in[1],
 	                                                               dims_in[2], accumulate);
 	g_kernel_launches++;
 	return BF_OK(cudaGetLastError());
@@ -515,15 +525,15 @@ uint32_t bf_unet_upsample2(const void *in, int32_t in_type, void *out, int32_t o
 	if (!in || !out || c <= 0 || !dims_out || dims_out[0] % 2 || dims_out[1] % 2 || dims_out[2] % 2) return 0;
 	cudaStream_t s = (cudaStream_t)stream;
 	const int W = dims_out[0], H = dims_out[1], D = dims_out[2];
-	const int64_t n = (int64_t)c * D * H * W;
+	const int g = grid_rows((int64_t)c * D * H), t = std::min(128, std::max(32, W));
 	if (in_type == BF_UNET_BF16 && out_type == BF_UNET_BF16)
-		upsample2_k<<<grid_for(n), 256, 0, s>>>((const __nv_bfloat16 *)in, (__nv_bfloat16 *)out, c, W, H, D);
+		upsample2_k<<<g, t, 0, s>>>((const __nv_bfloat16 *)in, (__nv_bfloat16 *)out, c, W, H, D);
 	else if (in_type == BF_UNET_F32 && out_type == BF_UNET_F32)
-		upsample2_k<<<grid_for(n), 256, 0, s>>>((const float *)in, (float *)out, c, W, H, D);
+		upsample2_k<<<g, t, 0, s>>>((const float *)in, (float *)out, c, W, H, D);
 	else if (in_type == BF_UNET_BF16)
-		upsample2_k<<<grid_for(n), 256, 0, s>>>((const __nv_bfloat16 *)in, (float *)out, c, W, H, D);
+		upsample2_k<<<g, t, 0, s>>>((const __nv_bfloat16 *)in, (float *)out, c, W, H, D);
 	else
-		upsample2_k<<<grid_for(n), 256, 0, s>>>((const float *)in, (__nv_bfloat16 *)out, c, W, H, D);
+		upsample2_k<<<g, t, 0, s>>>((const float *)in, (__nv_bfloat16 *)out, c, W, H, D);
 	g_kernel_launches++;
 	return BF_OK(cudaGetLastError());
 }
@@ -531,8 +541,9 @@ uint32_t bf_unet_upsample2(const void *in, int32_t in_type, void *out, int32_t o
 uint32_t bf_unet_upsample2_grad(const float *grad_out, float *grad_in, int32_t c, const int32_t dims_out[3], void *stream)
 {
 	if (!grad_out || !grad_in || c <= 0 || !dims_out) return 0;
-	const int64_t n = (int64_t)c * (dims_out[0] / 2) * (dims_out[1] / 2) * (dims_out[2] / 2);
-	upsample2_grad_k<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(grad_out, grad_in, c, dims_out[0], dims_out[1],
+	const int g = grid_rows((int64_t)c * (dims_out[2] / 2) * (dims_out[1] / 2));
+	const int t = std::min(128, std::max(32, dims_out[0] / 2));
+	upsample2_grad_k<<<g, t, 0, (cudaStream_t)stream>>>(grad_out, grad_in, c, dims_out[0], dims_out[1],
 	                                                                dims_out[2]);
 	g_kernel_launches++;
 	return BF_OK(cudaGetLastError());

@@ -594,30 +594,35 @@ __device__ __forceinline__ uint64_t interleaved(uint32_t addr, uint32_t lbo, uin
 /* channels-first [cin][V] (BF16, or FP32 rounded to BF16) -> planes [G][PR][8]:
  * plane g holds channels 8 g ... 8 g + 7 of every position P of the volume
  * padded by one zero voxel on each face ((D + 2) x (H + 2) x (W + 2), x
- * fastest), positions beyond it zero. Thread per (position, plane): 8 coalesced
- * loads, one 16-byte store (a warp stores 512 contiguous bytes). */
+ * fastest), positions beyond it zero. Block per (padded row, plane), threads
+ * over the row's positions: 8 coalesced loads and one 16-byte store each (a
+ * warp stores 512 contiguous bytes); the row arithmetic runs once per block. */
 template <typename TI>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(128)
 to_padded_planes(const TI *__restrict__ in, uint4 *__restrict__ planes, int cin, int W, int H, int D, int64_t PR)
 {
 	const int g = blockIdx.y;
-	const int Wp = W + 2;
-	const int64_t hw = (int64_t)(H + 2) * Wp, V = (int64_t)W * H * D;
-	for (int64_t P = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; P < PR; P += (int64_t)gridDim.x * blockDim.x) {
-		const int64_t zp = P / hw, rem = P - zp * hw;
-		const int yp = (int)(rem / Wp), xp = (int)(rem - (int64_t)yp * Wp);
-		uint32_t w[4] = {0u, 0u, 0u, 0u};
-		if (zp >= 1 && zp <= D && yp >= 1 && yp <= H && xp >= 1 && xp <= W) {
-			const int64_t v = ((zp - 1) * H + (yp - 1)) * (int64_t)W + (xp - 1);
-			#pragma unroll
-			for (int k = 0; k < 8; k += 2) {
-				const int c0 = g * 8 + k;
-				const uint32_t lo = c0 < cin ? bf16_bits(in, (int64_t)c0 * V + v) : 0u;
-				const uint32_t hi = c0 + 1 < cin ? bf16_bits(in, (int64_t)(c0 + 1) * V + v) : 0u;
-				w[k >> 1] = lo | (hi << 16);
+	const int Wp = W + 2, Hp = H + 2;
+	const int64_t V = (int64_t)W * H * D, rows = PR / Wp;
+	for (int64_t row = blockIdx.x; row < rows; row += gridDim.x) {
+		const int zp = (int)(row / Hp), yp = (int)(row - (int64_t)zp * Hp);
+		const bool inner = zp >= 1 && zp <= D && yp >= 1 && yp <= H;
+		const int64_t vrow = ((int64_t)(zp - 1) * H + (yp - 1)) * W - 1;    /* voxel of xp = 0 */
+		uint4 *dst = planes + (int64_t)g * PR + row * Wp;
+		for (int xp = threadIdx.x; xp < Wp; xp += blockDim.x) {
+			uint32_t w[4] = {0u, 0u, 0u, 0u};
+			if (inner && xp >= 1 && xp <= W) {
+				const int64_t v = vrow + xp;
+				#pragma unroll
+				for (int k = 0; k < 8; k += 2) {
+					const int c0 = g * 8 + k;
+					const uint32_t lo = c0 < cin ? bf16_bits(in, (int64_t)c0 * V + v) : 0u;
+					const uint32_t hi = c0 + 1 < cin ? bf16_bits(in, (int64_t)(c0 + 1) * V + v) : 0u;
+					w[k >> 1] = lo | (hi << 16);
+				}
 			}
+			dst[xp] = make_uint4(w[0], w[1], w[2], w[3]);
 		}
-		planes[(int64_t)g * PR + P] = make_uint4(w[0], w[1], w[2], w[3]);
 	}
 }
 
@@ -682,7 +687,7 @@ conv3d_slab(const __grid_constant__ ConvSlab p)
 	__syncthreads();
 	tc_fence_after();
 	const uint32_t tmem = tmem_slot;
-	const int64_t hw = (int64_t)p.Hp * p.Wp;
+	const uint32_t hw32 = (uint32_t)p.Hp * (uint32_t)p.Wp;
 	if (tid == 0 && p.resident) {
 		const uint32_t wb = (uint32_t)(9 * p.b_bytes);
 		asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(wbar), "r"(wb) : "memory");
@@ -766,11 +771,13 @@ conv3d_slab(const __grid_constant__ ConvSlab p)
 			if (lane == 0) ok = wait_role(afull0 + 8 * a, ua & 1, abort_flag);
 			if (!__shfl_sync(0xffffffffu, ok, 0)) break;
 			tc_fence_after();
-			const int64_t P = (int64_t)p.P0 + (int64_t)tile * TCM + quarter * 32 + lane;
-			const int64_t zp = P / hw, rem = P - zp * hw;
-			const int yp = (int)(rem / p.Wp), xp = (int)(rem - (int64_t)yp * p.Wp);
-			const bool inside = zp >= 1 && zp <= p.D && yp >= 1 && yp <= p.H && xp >= 1 && xp <= p.W;
-			const int64_t v = ((zp - 1) * p.H + (yp - 1)) * (int64_t)p.W + (xp - 1);
+			/* positions are below 2^31 (checked on the host): 32-bit division */
+			const uint32_t P = (uint32_t)p.P0 + (uint32_t)tile * TCM + quarter * 32 + lane;
+			const uint32_t zp = P / hw32, rem = P - zp * hw32;
+			const uint32_t yp = rem / (uint32_t)p.Wp, xp = rem - yp * (uint32_t)p.Wp;
+			const bool inside = zp >= 1 && zp <= (uint32_t)p.D && yp >= 1 && yp <= (uint32_t)p.H && xp >= 1 &&
+			                    xp <= (uint32_t)p.W;
+			const int64_t v = ((int64_t)(zp - 1) * p.H + (yp - 1)) * (int64_t)p.W + (xp - 1);
 			const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + a * (uint32_t)p.np;
 			for (int c0 = 0; c0 < p.np; c0 += 16) {
 				float acc[16];
@@ -923,8 +930,10 @@ bool conv3d_slab_launch(const void *in, int in_type, int cin, const uint16_t *w,
 	const int G = (cin + 15) / 16 * 2, np = (cout + 15) / 16 * 16;
 	if (np > 128) return false;
 	const int W = dims[0], H = dims[1], D = dims[2];
-	const int64_t Wp = W + 2, Hp = H + 2, Vp = (int64_t)(D + 2) * Hp * Wp;
-	const int64_t PR = Vp + 256;
+	const int64_t Wp = W + 2, Hp = H + 2;
+	/* whole padded rows, at least 256 positions past the volume (a tile's last
+	 * slab may read up to 127 + 2 positions beyond it) */
+	const int64_t PR = ((D + 2) * Hp + (256 + Wp - 1) / Wp) * Wp;
 	if (PR > INT32_MAX) return false;
 	ConvSlab p{};
 	p.a_bytes = G * SLAB_PLANE;
@@ -944,11 +953,12 @@ bool conv3d_slab_launch(const void *in, int in_type, int cin, const uint16_t *w,
 	    (const __nv_bfloat16 *)w, g_bk, cin, G, cout, np);
 	g_kernel_launches++;
 	if ((err = cudaGetLastError()) != cudaSuccess) return true;
-	const dim3 cgrid((unsigned)std::min<int64_t>((PR + 255) / 256, (int64_t)device_sm_count() * 16), (unsigned)G);
+	const dim3 cgrid((unsigned)std::min<int64_t>(PR / Wp, (int64_t)device_sm_count() * 32), (unsigned)G);
+	const int cthreads = Wp >= 128 ? 128 : (int)(Wp + 31) / 32 * 32;
 	if (in_type == BF_UNET_F32)
-		to_padded_planes<<<cgrid, 256, 0, s>>>((const float *)in, (uint4 *)g_cl, cin, W, H, D, PR);
+		to_padded_planes<<<cgrid, cthreads, 0, s>>>((const float *)in, (uint4 *)g_cl, cin, W, H, D, PR);
 	else
-		to_padded_planes<<<cgrid, 256, 0, s>>>((const uint16_t *)in, (uint4 *)g_cl, cin, W, H, D, PR);
+		to_padded_planes<<<cgrid, cthreads, 0, s>>>((const uint16_t *)in, (uint4 *)g_cl, cin, W, H, D, PR);
 	g_kernel_launches++;
 	if ((err = cudaGetLastError()) != cudaSuccess) return true;
 	p.planes = g_cl;

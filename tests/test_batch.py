@@ -69,3 +69,38 @@ def test_batch_rejects_coherency_weighting():
     with pytest.raises(BeamformerError):
         bf.beamform_batch(params, [t.data_ptr() for t in rf], [t.numel() * 2 for t in rf], [t.data_ptr() for t in out])
     assert bf.lib.beamformer_get_last_error() == abi.ERR["UNSUPPORTED"]
+
+
+def test_batch_volume_tiles_staged(monkeypatch):
+    """HERCULES tiles of the batch read the FP32 table staged in shared memory, as
+    the single launch does: with OGL_BF_DAS_STAGED=require a tile that could not
+    stage writes NaN. Two volumes with the 3D workload's voxel size (78 um x 78 um
+    x 78 um) and a plane; the batch output equals the plain API's (which may split
+    the receive channels into groups, so summation orders differ) to FP32 rounding."""
+    import torch
+    from ogl_beamforming_cuda_gb300 import synth
+    monkeypatch.setenv("OGL_BF_DAS_STAGED", "require")
+    lo, hi = np.array((-5e-3, -5e-3, 5e-3)), np.array((5e-3, 5e-3, 25e-3))
+    params, rf, out, single = [], [], [], []
+    for i, pts in enumerate(((32, 32, 64), (16, 32, 32), (48, 1, 64))):
+        mid, half = (lo + hi) / 2, (hi - lo) / 2 * np.asarray(pts) / np.array((128, 128, 256))
+        if pts[1] == 1:
+            half[1] = 0.0
+        bp = synth.make_parameters(samples=2048, channels=128, transmits=128, points=pts,
+                                   extent=(tuple(mid - half), tuple(mid + half)), decimation=2, f_number=1.0,
+                                   interpolate=1, frames=1, filter_length=64)
+        raw = synth.acquisition(bp, 40 + i, n_points=30, n_speckle=300)
+        params.append(bp)
+        rf.append(torch.from_numpy(raw).cuda())
+        out.append(torch.zeros(2 * int(np.prod(pts)), dtype=torch.float32, device="cuda"))
+        one = Beamformer().configure(bp, PIPE, kaiser=synth.kaiser_spec(64))
+        one.push(raw)
+        one.synchronize()
+        single.append(one.frame(0)[0].copy())
+    bf = Beamformer().configure(params[0], PIPE, kaiser=synth.kaiser_spec(64))
+    bf.beamform_batch(params, [t.data_ptr() for t in rf], [t.numel() * 2 for t in rf], [t.data_ptr() for t in out])
+    for i, (o, ref) in enumerate(zip(out, single)):
+        got = o.cpu().numpy()
+        assert np.all(np.isfinite(got)), f"acquisition {i}: a tile did not stage"
+        assert np.max(np.abs(got - ref.ravel())) <= 1e-5 * np.max(np.abs(ref)), f"acquisition {i}"
+
