@@ -549,14 +549,26 @@ __device__ __forceinline__ void hercules_staged_body(const DasParams &p, const f
 			float2 acc[2] = {make_float2(ax[0], ay[0]), make_float2(ax[NV - 1], ay[NV - 1])};
 			const float2 dz2p = make_float2(v[0].dz2, v[NV - 1].dz2), ka2p = make_float2(v[0].ka2, v[NV - 1].ka2);
 			const float2 dtxp = make_float2(v[0].dtx, v[NV - 1].dtx);
-			#pragma unroll 1
-			for (; t <= te; t++) {
-				const int slot = t - ct0;
-				const int lo = win_lo[buf * RC + slot];
-				const float dv = __fsub_rn(q_var, __fmul_rn((float)t, pitch_var));
+			if (t == 0 && t <= te) {
+				/* transmit 0 carries the 1 / sqrt(T) weight: peeled, so the loop below
+				 * has no per-term scale */
+				const float dv = __fsub_rn(q_var, __fmul_rn(0.0f, pitch_var));
 				const float lat2 = __fadd_rn(f2, __fmul_rn(dv, dv));
-				stg_term2<INTERP, DEMOD, ROT, WM>(p, (const float4 *)(base + slot * WM * SEGB), lo, lat2, dz2p, ka2p,
-				                                  dtxp, t == 0 ? p.inv_sqrt_T : 1.0f, acc);
+				/* t == 0 >= ct0: the chunk's first row */
+				stg_term2<INTERP, DEMOD, ROT, WM>(p, (const float4 *)base, win_lo[buf * RC], lat2, dz2p, ka2p, dtxp,
+				                                  p.inv_sqrt_T, acc);
+				t = 1;
+			}
+			/* per term: the row's window through pointers stepped by one row, and t as
+			 * a float counter (exact: t < 2^24, so the products are the ones (float)t gives) */
+			const int *wl = win_lo + buf * RC + (t - ct0);
+			const float4 *wrow = (const float4 *)(base + (t - ct0) * WM * SEGB);
+			float tf = (float)t;
+			#pragma unroll 1
+			for (; t <= te; t++, wl++, wrow += WM * SEGB / 16, tf += 1.0f) {
+				const float dv = __fsub_rn(q_var, __fmul_rn(tf, pitch_var));
+				const float lat2 = __fadd_rn(f2, __fmul_rn(dv, dv));
+				stg_term2<INTERP, DEMOD, ROT, WM>(p, wrow, *wl, lat2, dz2p, ka2p, dtxp, 1.0f, acc);
 			}
 			ax[0] = acc[0].x; ay[0] = acc[0].y; ax[NV - 1] = acc[1].x; ay[NV - 1] = acc[1].y;
 		} else {
