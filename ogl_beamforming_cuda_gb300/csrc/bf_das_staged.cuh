@@ -564,7 +564,7 @@ __device__ __forceinline__ void hercules_staged_body(const DasParams &p, const f
 			const int *wl = win_lo + buf * RC + (t - ct0);
 			const float4 *wrow = (const float4 *)(base + (t - ct0) * WM * SEGB);
 			float tf = (float)t;
-			#pragma unroll 1
+			#pragma unroll 2
 			for (; t <= te; t++, wl++, wrow += WM * SEGB / 16, tf += 1.0f) {
 				const float dv = __fsub_rn(q_var, __fmul_rn(tf, pitch_var));
 				const float lat2 = __fadd_rn(f2, __fmul_rn(dv, dv));
@@ -582,16 +582,18 @@ __device__ __forceinline__ void hercules_staged_body(const DasParams &p, const f
 					                                 p.inv_sqrt_T, ax[k], ay[k]);
 				t = 1;
 			}
+			/* as the packed loop: row pointers stepped, t as an exact float counter */
+			const int *wl = win_lo + buf * RC + (t - ct0);
+			const float4 *wrow = (const float4 *)(base + (t - ct0) * WM * SEGB);
+			float tf = (float)t;
 			#pragma unroll 2
-			for (; t <= te; t++) {
-				const int slot = t - ct0;
-				const int lo = win_lo[buf * RC + slot];
-				const float dv = __fsub_rn(q_var, __fmul_rn((float)t, pitch_var));
+			for (; t <= te; t++, wl++, wrow += WM * SEGB / 16, tf += 1.0f) {
+				const int lo = *wl;
+				const float dv = __fsub_rn(q_var, __fmul_rn(tf, pitch_var));
 				const float lat2 = __fadd_rn(f2, __fmul_rn(dv, dv));
-				const float4 *win = (const float4 *)(base + slot * WM * SEGB);
 				#pragma unroll
 				for (int k = 0; k < NV; k++)
-					stg_term<INTERP, DEMOD, ROT, WM>(p, win, lo, lat2, v[k].dz2, v[k].ka2, v[k].dtx, 1.0f, ax[k], ay[k]);
+					stg_term<INTERP, DEMOD, ROT, WM>(p, wrow, lo, lat2, v[k].dz2, v[k].ka2, v[k].dtx, 1.0f, ax[k], ay[k]);
 			}
 		}
 		if (!has_next || nr != cr) {
