@@ -537,12 +537,19 @@ __device__ __forceinline__ void hercules_staged_body(const DasParams &p, const f
 			float2 hx = make_float2(ax[0], ax[NV - 1]), hy = make_float2(ay[0], ay[NV - 1]);
 			const float2 dz2h = make_float2(v[0].dz2, v[NV - 1].dz2), ka2h = make_float2(v[0].ka2, v[NV - 1].ka2);
 			const float2 ioh = make_float2(v[0].io, v[NV - 1].io);
-			for (; t <= te; t++) {
-				const int slot = t - ct0;
-				const int lo = win_lo[buf * RC + slot];
-				const float dv = fmaf(-(float)t, pitch_var, q_var);
-				stg_term_h2<INTERP, DEMOD, ROT, WM>(p, base + slot * WM * SEGB, lo, fmaf(dv, dv, f2), dz2h, ka2h, ioh,
-				                                    t == 0 ? p.inv_sqrt_T : 1.0f, hx, hy);
+			if (t == 0 && t <= te) {
+				/* t == 0 >= ct0: the chunk's first row, with the 1 / sqrt(T) weight */
+				stg_term_h2<INTERP, DEMOD, ROT, WM>(p, base, win_lo[buf * RC], fmaf(q_var, q_var, f2), dz2h, ka2h, ioh,
+				                                    p.inv_sqrt_T, hx, hy);
+				t = 1;
+			}
+			const int *wl = win_lo + buf * RC + (t - ct0);
+			const uint8_t *wrow = base + (t - ct0) * WM * SEGB;
+			float tf = (float)t;
+			#pragma unroll 2
+			for (; t <= te; t++, wl++, wrow += WM * SEGB, tf += 1.0f) {
+				const float dv = fmaf(-tf, pitch_var, q_var);
+				stg_term_h2<INTERP, DEMOD, ROT, WM>(p, wrow, *wl, fmaf(dv, dv, f2), dz2h, ka2h, ioh, 1.0f, hx, hy);
 			}
 			ax[0] = hx.x; ax[NV - 1] = hx.y; ay[0] = hy.x; ay[NV - 1] = hy.y;
 		} else if (NV == 2) {
