@@ -32,6 +32,16 @@ def test_library_exports_every_declared_symbol(lib):
     assert set(abi.REFERENCE_SYMBOLS) <= exported and len(abi.REFERENCE_SYMBOLS) == 24
 
 
+def test_library_exports_every_unet_symbol(lib):
+    """include/bf_unet.h (the learned variant's kernels): every declared function is exported."""
+    text = open(os.path.join(ROOT, "include", "bf_unet.h")).read()
+    names = sorted(set(re.findall(r"^uint32_t\s+(\w+)\s*\(", text, re.M)))
+    assert {"bf_unet_conv3d", "bf_unet_conv3d_grad_input", "bf_unet_ema", "bf_unet_tc_errors"} <= set(names)
+    out = subprocess.run(["nm", "-D", "--defined-only", abi.LIB_PATH], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    assert set(names) <= exported, sorted(set(names) - exported)
+
+
 @pytest.mark.skipif(not os.path.exists(REF_CLIENT), reason="reference client library not built")
 def test_reference_exports_are_a_subset():
     out = subprocess.run(["nm", "-D", "--defined-only", REF_CLIENT], capture_output=True, text=True).stdout
