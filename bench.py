@@ -226,6 +226,27 @@ def fp32_peak_tflops(peaks, sms):
     return sms * 128 * 2 * mhz * 1e6 / 1e12
 
 
+def support_fraction(f_number=1.0, step=4):
+    """Share of the workload's (transmit, receive) pairs inside the apodization
+    support (lateral distance below z / (2 f_number)), over every `step`-th voxel
+    per axis: the terms the DAS kernels skip have weight exactly 0 and are still
+    counted in the algorithmic sample-ops, as the reference visits them."""
+    from ogl_beamforming_cuda_gb300 import synth
+    lo, hi = np.asarray(WORKLOAD_EXTENT[0]), np.asarray(WORKLOAD_EXTENT[1])
+    axes = [np.linspace(lo[k], hi[k], POINTS[k])[::step] for k in range(3)]
+    rx = (np.arange(C) - (C - 1) / 2) * synth.PITCH
+    tx = (np.arange(T) - (T - 1) / 2) * synth.PITCH
+    x, y, z = np.meshgrid(*axes, indexing="ij")
+    r2 = (z / (2 * f_number)) ** 2
+    inside = 0
+    for e in rx:                          # per receive element: a transmit interval
+        h2 = r2 - (x - e) ** 2
+        h = np.sqrt(np.maximum(h2, 0.0))
+        n = (np.searchsorted(tx, (y + h).ravel(), "left") - np.searchsorted(tx, (y - h).ravel(), "right"))
+        inside += np.sum(np.where(h2.ravel() > 0, np.maximum(n, 0), 0))
+    return float(inside) / (x.size * C * T)
+
+
 def das_roofline(das_t, peaks, traffic, shared_gbs, sms):
     """DAS is bound by min(FP32 peak / 40 flops, L1 bandwidth / 32 B) per cubic
     sample-op (one (voxel, transmit, receive) term); for cubic the L1 term is the
@@ -252,6 +273,10 @@ def das_roofline(das_t, peaks, traffic, shared_gbs, sms):
         out.update(bound="fp32", unit="TFLOP/s", peak=fp32,
                    achieved=ops * DAS_FLOPS_PER_TERM / das_t / 1e12 if das_t else None)
     out["frac"] = out["achieved"] / out["peak"] if das_t else None
+    out["apodization_support_fraction"] = support_fraction()
+    out["note"] = ("sample_ops counts every (voxel, transmit, receive) term, as the reference visits them; the "
+                   "kernel skips the terms outside the apodization support (weight exactly 0), the share "
+                   "1 - apodization_support_fraction of them")
     out["fp32_tflops"] = ops * DAS_FLOPS_PER_TERM / das_t / 1e12 if das_t else None
     out["fp32_frac"] = out["fp32_tflops"] / fp32 if das_t else None
     return out
