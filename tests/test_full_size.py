@@ -196,10 +196,13 @@ def test_volume_workload_every_block_staged(monkeypatch):
     rf = front["channel_data"][: plan.rf_size // 4]
     V, per = int(np.prod(dims)), 256
     out = np.zeros(2 * V, np.float32)
-    got, exp = [], []
+    got, got16, exp = [], [], []
     for i in range(8):
         v0 = (V // 8) * i + 4096 * (i % 4)
         O.das(plan.das, rf, dims, orc.sparse, orc.focal, fast=True, voxel_begin=v0, voxel_end=v0 + per, out=out)
         got.append(vols[0][2 * v0: 2 * (v0 + per)])
+        got16.append(vols[1][2 * v0: 2 * (v0 + per)])
         exp.append(out[2 * v0: 2 * (v0 + per)].copy())
     check_volume(np.concatenate(got), np.concatenate(exp), "3D workload, staged blocks only")
+    # the FP16 table against the oracle itself (not only against the FP32 volume)
+    assert nrmse(np.concatenate(got16), np.concatenate(exp)) <= -50.0
