@@ -12,6 +12,8 @@ the CPU oracle (the reference's semantics) on the same seeded int16 RF.
   oracle's Sum and MinMax of the GPU's own frames.
 - Precision workload front end: S = 4096, 128 taps; FP32 against the oracle,
   FP16 / BF16 (tensor-core FIR) against the FP64 restatement, with the plane.
+- FORCES at the batched workload's largest size (128 x 128 x 256 cubic,
+  T = C = 128, S = 2048) through its fast path, on stratified voxel runs.
 
 Tolerances: decode, Sum and MinMax bit-exact; the float stages NRMSE <= -80 dB
 and max |err| <= 1e-4 of the peak against the oracle; FP16 <= -65 dB and BF16
@@ -206,3 +208,37 @@ def test_volume_workload_every_block_staged(monkeypatch):
     check_volume(np.concatenate(got), np.concatenate(exp), "3D workload, staged blocks only")
     # the FP16 table against the oracle itself (not only against the FP32 volume)
     assert nrmse(np.concatenate(got16), np.concatenate(exp)) <= -50.0
+
+
+def test_forces_volume_full_size_stratified():
+    """FORCES at the batched workload's largest size: 128 x 128 x 256 cubic volume,
+    T = C = 128, S = 2048, through the FORCES fast path (per-frame table,
+    in-range proof) with its channel groups; stratified voxel runs against the
+    oracle."""
+    bp = synth.make_parameters(samples=2048, channels=128, transmits=128, points=(128, 128, 256), decimation=2,
+                               f_number=1.0, interpolate=1, das_id="FORCES", filter_length=64)
+    bp.output_points[3] = 1
+    kaiser = synth.kaiser_spec(64)
+    dims = (128, 128, 256)
+    raw = synth.acquisition(bp, 23, n_points=60, n_speckle=600, device="cuda")
+    bf = Beamformer().configure(bp, PIPE, kaiser=kaiser)
+    bf.push(raw)
+    bf.synchronize()
+    vol = bf.frame(0)[0].copy()
+    assert np.all(np.isfinite(vol))
+    orc = oracle_for(bf, bp, PIPE, kaiser=kaiser)
+    orc.shaders = [SH["Decode"], SH["Demodulate"]]
+    front = orc.compute(raw)
+    plan = O.plan(bp, PIPE, [0] * len(PIPE), abi.DATA_KIND["Int16"],
+                  [(0, kaiser[3], kaiser[2], kaiser[0], kaiser[1]), None, None, None])
+    rf = front["channel_data"][: plan.rf_size // 4]
+    V, per = int(np.prod(dims)), 128
+    out = np.zeros(2 * V, np.float32)
+    got, exp = [], []
+    for i in range(8):
+        v0 = (V // 8) * i + 8192 * (i % 4) + 64
+        O.das(plan.das, rf, dims, orc.sparse, orc.focal, fast=True, voxel_begin=v0, voxel_end=v0 + per, out=out)
+        got.append(vol[2 * v0: 2 * (v0 + per)])
+        exp.append(out[2 * v0: 2 * (v0 + per)].copy())
+    check_volume(np.concatenate(got), np.concatenate(exp), "FORCES 128 x 128 x 256, stratified voxels")
+

@@ -115,6 +115,28 @@ def test_conv_forward_tma_tiles(k, monkeypatch, cin, cout, dims, out_type, resid
             assert np.abs(outs[0] - o).max() <= 1e-5 * np.abs(ref).max()
 
 
+def test_conv_forward_full_resolution_slab_against_direct(k, monkeypatch):
+    """The network's largest layer at full size (48 -> 16 channels, 128 x 128 x 256):
+    the slab form (tensor cores) against the direct FP32 kernel, every voxel; FP32
+    sums of 1296 products each in two orders."""
+    g = torch.Generator(device="cuda").manual_seed(5)
+    cin, cout, dims = 48, 16, (128, 128, 256)
+    W, H, D = dims
+    x = torch.randn((cin, D, H, W), device="cuda", generator=g).to(torch.bfloat16)
+    w = (torch.randn(cout * cin * 27, device="cuda", generator=g) * 0.05).to(torch.bfloat16)
+    b = torch.randn(cout, device="cuda", generator=g)
+    outs = []
+    for simt in ("0", "1"):
+        monkeypatch.setenv("OGL_BF_UNET_SIMT", simt)
+        monkeypatch.delenv("OGL_BF_UNET_TC", raising=False)
+        out = torch.empty((cout, D, H, W), dtype=torch.float32, device="cuda")
+        k.conv(x, cin, w, b, out, cout, dims, True)
+        outs.append(out)
+    assert k.lib.bf_unet_tc_errors(k.stream) == 0
+    diff = (outs[0] - outs[1]).abs().max().item()
+    assert diff <= 1e-5 * outs[1].abs().max().item()
+
+
 def test_conv_grad_input(k, monkeypatch):
     """the direct kernel (FP32 products)"""
     monkeypatch.setenv("OGL_BF_UNET_SIMT", "1")
