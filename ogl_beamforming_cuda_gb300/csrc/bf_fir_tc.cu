@@ -26,9 +26,11 @@
  * tensor memory, double-buffered columns) and commits to an mbarrier; all four
  * warps read their 32 accumulator lanes with tcgen05.ld, rotate by e^{i theta n D},
  * stage the rows in a padded shared-memory tile and store complex f32 [row][n] as
- * whole row segments (16 bytes per lane, coalesced). The next block's MMAs are issued before the
- * epilogue of the current one. Every wait is bounded (about one second); a wait
- * that runs out sets the error word and the CTA stops after draining its loads.
+ * whole row segments (16 bytes per lane, coalesced). The next block's MMAs are
+ * issued before the epilogue of the current one; each warp releases an
+ * accumulator buffer on an mbarrier once it has read it (no block-wide barrier
+ * per block). Every wait is bounded (about one second); a wait that runs out
+ * sets the error word and the CTA stops after draining its loads.
  */
 #include "bf_kernels.h"
 
@@ -168,9 +170,9 @@ fir_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtenso
 	uint8_t *ring = smem;                                        /* TC_RING atoms */
 	uint8_t *gsm  = ring + TC_RING * TC_ATOM_BYTES;              /* atoms x (N rows x 128 B) */
 	uint64_t *bars = (uint64_t *)(gsm + (size_t)p.atoms * N * 128);
-	float4 *epi = (float4 *)(bars + TC_RING + 4);              /* 4 warps x 32 rows x (N / 4 + 1) chunks */
+	float4 *epi = (float4 *)(bars + TC_RING + 6);              /* 4 warps x 32 rows x (N / 4 + 1) chunks */
 	__shared__ uint32_t tmem_slot;
-	__shared__ int stop;
+	__shared__ volatile int stop;
 
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const int rb = blockIdx.x / p.splits, split = blockIdx.x - rb * p.splits;
@@ -183,6 +185,7 @@ fir_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtenso
 
 	const uint32_t full0 = smem_u32(bars), mma0 = smem_u32(bars + TC_RING), gbar = smem_u32(bars + TC_RING + 2);
 	const uint32_t never = smem_u32(bars + TC_RING + 3);        /* no thread or copy arrives here */
+	const uint32_t aempty0 = smem_u32(bars + TC_RING + 4);      /* accumulator buffer read by all 4 warps */
 	/* two accumulator buffers of N f32 columns; allocations are powers of two >= 32 */
 	constexpr uint32_t tcols = N <= 16 ? 32u : N <= 32 ? 64u : 128u;
 	if (warp == 0) {
@@ -196,6 +199,8 @@ fir_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtenso
 		mbar_init(mma0 + 8, 1);
 		mbar_init(gbar, 1);
 		mbar_init(never, 1);
+		mbar_init(aempty0, 4);
+		mbar_init(aempty0 + 8, 4);
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 		stop = 0;
 	}
@@ -237,11 +242,21 @@ fir_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtenso
 	}
 	__syncthreads();
 
+	/* No block-wide barrier per block: a warp releases accumulator buffer i % 2
+	 * (one arrival on its "empty" mbarrier) once it has read it, and thread 0 waits
+	 * for that before the MMAs of block i + 2 overwrite it; an input atom's slot is
+	 * refilled as soon as the MMAs of the last block reading it are complete. */
 	for (int i = 0; i < nq && !stop; i++) {
-		if (tid == 0 && i + 1 < nq && !mma_block(i + 1)) stop = 1;
+		if (tid == 0 && i + 1 < nq) {
+			/* buffer (i + 1) % 2 last held block i - 1 */
+			if (i >= 1 && !mbar_wait(aempty0 + 8 * ((i + 1) & 1), (uint32_t)(((i - 1) >> 1) & 1))) stop = 1;
+			else if (!mma_block(i + 1)) stop = 1;
+		}
 		/* every thread: accumulators of block i */
 		const bool done = __all_sync(0xFFFFFFFFu, mbar_wait(mma0 + 8 * (i & 1), (uint32_t)((i >> 1) & 1)));
 		tc_fence_after();
+		/* block i's MMAs are complete: its first atom's slot takes atom i + TC_RING */
+		if (tid == 0 && done && !stop && issued < total_atoms) issue_atom(issued++);
 		if (done) {
 			/* this warp's lanes, the N columns of accumulator buffer i % 2 */
 			float v[64];
@@ -252,6 +267,9 @@ fir_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtenso
 				tmem_ld32(ta, v);
 				if (N == 64) tmem_ld32(ta + 32, v + 32);
 			}
+			tc_fence_before();
+			__syncwarp();
+			if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(aempty0 + 8 * (i & 1)) : "memory");
 			/* rotate this lane's row into the warp's staging tile (row = lane, 16-byte
 			 * chunks of two outputs, rows padded by one chunk: conflict-free both ways),
 			 * then store whole row segments: CPR lanes per row, 32 / CPR rows per
@@ -287,10 +305,6 @@ fir_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtenso
 		} else {
 			stop = 1;
 		}
-		tc_fence_before();
-		__syncthreads();
-		/* block i's MMAs are complete: its first atom's slot takes atom i + TC_RING */
-		if (tid == 0 && !stop && issued < total_atoms) issue_atom(issued++);
 	}
 	__syncthreads();
 	if (tid == 0 && stop) {
@@ -433,7 +447,7 @@ cudaError_t launch_fir_tc(const void *x, uint32_t rows, uint32_t row_samples, ui
 	splits = std::min(splits, std::max(1, p.q_blocks / 4));
 	p.splits = splits;
 	p.vec_store = (n_out % 2 == 0 && ((uintptr_t)out & 15) == 0) ? 1 : 0;
-	const size_t smem = 1024 + (size_t)TC_RING * TC_ATOM_BYTES + (size_t)p.atoms * N * 128 + (TC_RING + 4) * 8 +
+	const size_t smem = 1024 + (size_t)TC_RING * TC_ATOM_BYTES + (size_t)p.atoms * N * 128 + (TC_RING + 6) * 8 +
 	                    (size_t)4 * 32 * (N / 4 + 1) * 16;
 	/* the dynamic shared memory this launch needs, within the device's opt-in limit
 	 * less the kernel's static shared memory */
