@@ -742,11 +742,14 @@ conv3d_slab(const __grid_constant__ ConvSlab p)
 					tc_fence_after();
 					const uint32_t a0 = su32(stages + (size_t)s * p.stage_bytes);
 					const uint32_t b0 = p.resident ? su32(wres) + (uint32_t)(sl * p.b_bytes) : a0 + (uint32_t)p.a_bytes;
+					/* the descriptors of one stage differ only in their start field (16-byte
+					 * units, bits 0-13; shared addresses stay below 2^18): built once, offset per MMA */
+					const uint64_t da0 = interleaved(a0, SLAB_PLANE, 128), db0 = interleaved(b0, bplane, 128);
 					for (int dx = 0; dx < 3; dx++)
 						for (int j = 0; j < p.G; j += 2) {
 							const uint32_t acc = (sl | dx | j) != 0;
-							const uint64_t da = interleaved(a0 + j * SLAB_PLANE + dx * 16, SLAB_PLANE, 128);
-							const uint64_t db = interleaved(b0 + (uint32_t)(dx * p.G + j) * bplane, bplane, 128);
+							const uint64_t da = da0 + (uint64_t)((uint32_t)(j * SLAB_PLANE + dx * 16) >> 4);
+							const uint64_t db = db0 + (uint64_t)(((uint32_t)(dx * p.G + j) * bplane) >> 4);
 							asm volatile("{\n\t.reg .pred q;\n\t"
 							             "setp.ne.b32 q, %4, 0;\n\t"
 							             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, q;\n\t}"
